@@ -1,0 +1,167 @@
+"""Python mirror of the reference's filtering interface, on top of the C ABI.
+
+Reference surface (header-only CUDA, compile-time configured):
+  setup_kernel_coefficients(sos)               include/ph_kernels.cuh:151 (and stcr/dtcr/plr)
+  KERNEL_FUNC<<<grid, block>>>(in, out, status, partcarry, fullcarry, launch)
+                                               src/test_accuracy.cu:146
+Here a :class:`Plan` owns what the reference's caller allocated (status / carries / launch
+index); realization and BLOCK_SIZE x N_BLOCKS are constructor arguments. Device memory and
+streams come from PyTorch; the filtering itself is the CUDA library (no fallback).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import KERNELS, KERNEL_NAMES, IirError, check
+
+__all__ = ["Plan", "PlrPlan", "sosfilt", "KERNELS", "IirError"]
+
+
+def _kernel_id(kernel) -> int:
+    if isinstance(kernel, str):
+        k = kernel.upper()
+        if k not in KERNELS:
+            raise ValueError(f"unknown realization {kernel!r}; one of {sorted(KERNELS)}")
+        return KERNELS[k]
+    return int(kernel)
+
+
+def _sos_array(sos) -> np.ndarray:
+    s = np.ascontiguousarray(np.asarray(sos, dtype=np.float32).reshape(-1, 6))
+    if s.shape[0] < 1:
+        raise ValueError("sos needs at least one section")
+    return s
+
+
+def _stream_handle(stream) -> ctypes.c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(int(stream.cuda_stream))
+
+
+def _check_tensor(x: torch.Tensor, name: str) -> None:
+    if not isinstance(x, torch.Tensor) or not x.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if x.dtype != torch.float32:
+        raise TypeError(f"{name} must be float32")
+    if not x.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+class Plan:
+    """A filter bound to a realization and geometry (the reference's compile-time choice).
+
+    Parameters mirror the reference's build variables: ``kernel`` = KERNEL (PH / STCR /
+    STCR_UNROLL / DTCR / DTCR_UNROLL / PLR / AUTO), ``block_size`` = BLOCK_SIZE,
+    ``n_blocks`` = N_BLOCKS (PLR: values per thread), 0 = tuned default.
+    The plan's status buffer is zeroed once here and never reset (launch-versioned flags).
+    Launches must be issued from one stream at a time.
+    """
+
+    def __init__(self, sos, kernel="AUTO", block_size: int = 0, n_blocks: int = 0, max_n: int = 1 << 20,
+                 device=None):
+        self._lib = _lib.load()
+        self._sos = _sos_array(sos)
+        self._ptr = ctypes.c_void_p()
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.device = dev
+        with torch.cuda.device(dev):
+            st = self._lib.iir_plan_create(ctypes.byref(self._ptr),
+                                           self._sos.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                           self._sos.shape[0], _kernel_id(kernel), int(block_size), int(n_blocks),
+                                           int(max_n))
+        check(st, "iir_plan_create")
+
+    @classmethod
+    def _from_ptr(cls, ptr, device):
+        obj = cls.__new__(cls)
+        obj._lib = _lib.load()
+        obj._ptr = ptr
+        obj.device = device
+        obj._sos = None
+        return obj
+
+    def info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(5)]
+        check(self._lib.iir_plan_info(self._ptr, *[ctypes.byref(v) for v in vals]), "iir_plan_info")
+        k, b, n, g, s = (v.value for v in vals)
+        return {"kernel": KERNEL_NAMES.get(k, k), "block_size": b, "n_blocks": n, "grid": g, "n_sections": s}
+
+    def __call__(self, x: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        _check_tensor(x, "x")
+        if out is None:
+            out = torch.empty_like(x)
+        _check_tensor(out, "out")
+        if out.numel() != x.numel():
+            raise ValueError("out must have as many samples as x")
+        st = self._lib.iir_plan_execute(self._ptr, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                        x.numel(), _stream_handle(stream))
+        check(st, "iir_plan_execute")
+        return out
+
+    def check(self, stream=None) -> None:
+        """Synchronises the stream and raises IirError if a launch recorded a device error."""
+        check(self._lib.iir_plan_check(self._ptr, _stream_handle(stream)), "device")
+
+    def set_timeout_ns(self, ns: int) -> None:
+        check(self._lib.iir_plan_set_timeout_ns(self._ptr, int(ns)))
+
+    def debug_withhold(self, chunk: int) -> None:
+        check(self._lib.iir_plan_debug_withhold(self._ptr, int(chunk)))
+
+    def close(self) -> None:
+        if getattr(self, "_ptr", None) is not None and self._ptr.value:
+            self._lib.iir_plan_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PlrPlan(Plan):
+    """PLR plan from direct-form taps (filter_taps.hpp PLR_FILTER_B / PLR_FILTER_A)."""
+
+    def __init__(self, b, a, gain: float = 1.0, block_size: int = 0, values_per_thread: int = 0,
+                 max_n: int = 1 << 20, device=None):
+        self._lib = _lib.load()
+        self._sos = None
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if b.shape != a.shape:
+            raise ValueError("b and a must have the same length (the order)")
+        self._ptr = ctypes.c_void_p()
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.device = dev
+        dp = ctypes.POINTER(ctypes.c_double)
+        with torch.cuda.device(dev):
+            st = self._lib.iir_plan_create_plr_ba(ctypes.byref(self._ptr), b.ctypes.data_as(dp), a.ctypes.data_as(dp),
+                                                  b.size, float(gain), int(block_size), int(values_per_thread),
+                                                  int(max_n))
+        check(st, "iir_plan_create_plr_ba")
+
+
+def sosfilt(sos, x: torch.Tensor, kernel="AUTO", block_size: int = 0, n_blocks: int = 0,
+            out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """One-shot cascaded-biquad filtering of a CUDA float32 signal (zero initial state).
+
+    ``sos`` rows are scipy's {b0, b1, b2, a0, a1, a2}; they are normalised in FP64 and the
+    removed gain is applied to the input. Plans are cached per (stream, filter, realization).
+    """
+    lib = _lib.load()
+    s = _sos_array(sos)
+    _check_tensor(x, "x")
+    if out is None:
+        out = torch.empty_like(x)
+    _check_tensor(out, "out")
+    st = lib.iir_sos_filter_geom(ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), x.numel(),
+                                 s.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), s.shape[0], _kernel_id(kernel),
+                                 int(block_size), int(n_blocks), _stream_handle(stream))
+    check(st, "iir_sos_filter")
+    return out

@@ -1,0 +1,679 @@
+// iir_host.cu — host planner and C ABI (include/iir_gb300.h).
+//
+// Replaces the reference's per-header setup_kernel_coefficients (ph_kernels.cuh:151-200,
+// stcr_kernels.cuh:191-272, dtcr_kernels.cuh:203-289, plr_kernels.cuh:416-476) and the
+// buffers its drivers allocate (src/test_accuracy.cu:136-147):
+//   * SOS rows are normalised in FP64 (b0 = a0 = 1) and rounded to float32 once; the
+//     removed gain multiplies the input in the kernel (FILTER_GAIN, src/test_accuracy.cu:120-124);
+//   * every derived table (state-transition powers C^k, chunk transition powers Q^l, cyclic-
+//     reduction factors, PLR n-nacci factors) is computed in FP64 from those float32
+//     coefficients, then rounded (the reference computes them in float32, T = float,
+//     include/iir_utils.hpp:22);
+//   * a plan owns the launch state (epoch = launch index, ticket counter), the flag|value
+//     carry slots zeroed once at allocation, and the lane tables.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/iir_gb300.h"
+#include "iir_params.h"
+#include "iir_registry.h"
+
+using namespace iirgb;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// kernel registry
+// ---------------------------------------------------------------------------------------
+std::vector<KernelEntry>& registry() {
+    static std::vector<KernelEntry> reg;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        register_ph(reg);
+        register_stcr(reg);
+        register_dtcr(reg);
+        register_plr(reg);
+    });
+    return reg;
+}
+
+const KernelEntry* find_entry(int kind, int B, int N, int order) {
+    for (const KernelEntry& e : registry())
+        if (e.kind == kind && e.B == B && e.N == N && e.order == order) return &e;
+    return nullptr;
+}
+
+struct OccKey {
+    int device;
+    const void* fn;
+    bool operator<(const OccKey& o) const { return std::tie(device, fn) < std::tie(o.device, o.fn); }
+};
+
+// Resident blocks per SM (all blocks of a persistent launch are co-resident).
+int blocks_per_sm(const KernelEntry& e, int device) {
+    static std::mutex mu;
+    static std::map<OccKey, int> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(OccKey{device, e.fn});
+    if (it != cache.end()) return it->second;
+    cudaFuncSetAttribute(e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(e.smem));
+    cudaFuncSetAttribute(e.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e.fn, e.threads, e.smem) != cudaSuccess) {
+        cudaGetLastError();
+        nb = 0;
+    }
+    cache[OccKey{device, e.fn}] = nb;
+    return nb;
+}
+
+// ---------------------------------------------------------------------------------------
+// FP64 2x2 algebra (row-major; acts on column vectors (y[n-2], y[n-1]))
+// ---------------------------------------------------------------------------------------
+struct M2 {
+    double a, b, c, d;
+};
+M2 mmul(const M2& x, const M2& y) {
+    return {x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+M2 mpow(M2 x, unsigned long long e) {
+    M2 r{1, 0, 0, 1};
+    while (e) {
+        if (e & 1ull) r = mmul(r, x);
+        x = mmul(x, x);
+        e >>= 1;
+    }
+    return r;
+}
+float4 to_f4(const M2& m) {
+    return make_float4(static_cast<float>(m.a), static_cast<float>(m.b), static_cast<float>(m.c),
+                       static_cast<float>(m.d));
+}
+int ilog2(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+
+struct SectionF32 {
+    float b1, b2, a1, a2;
+};
+
+// Normalises scipy SOS rows {b0,b1,b2,a0,a1,a2} to b0 = a0 = 1 (FP64), returns the removed
+// gain prod(b0/a0). Reference convention: ph_kernels.cuh:157-161, tools/ref_generate.py:62-67.
+int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out, double& gain) {
+    out.clear();
+    gain = 1.0;
+    for (int s = 0; s < n_sections; ++s) {
+        const double b0 = sos[6 * s + 0], b1 = sos[6 * s + 1], b2 = sos[6 * s + 2];
+        const double a0 = sos[6 * s + 3], a1 = sos[6 * s + 4], a2 = sos[6 * s + 5];
+        if (!(std::isfinite(b0) && std::isfinite(b1) && std::isfinite(b2) && std::isfinite(a0) &&
+              std::isfinite(a1) && std::isfinite(a2)))
+            return IIR_ERR_INVALID_ARGUMENT;
+        if (a0 == 0.0) return IIR_ERR_INVALID_ARGUMENT;
+        if (b0 == 0.0) return IIR_ERR_UNSUPPORTED;  // section gain cannot be factored out
+        gain *= b0 / a0;
+        out.push_back(SectionF32{static_cast<float>(b1 / b0), static_cast<float>(b2 / b0),
+                                 static_cast<float>(-a1 / a0), static_cast<float>(-a2 / a0)});
+    }
+    return IIR_OK;
+}
+
+// Fills one IirSection and its lane tables for geometry B x N.
+int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSection& q, float4* tab) {
+    std::memset(&q, 0, sizeof(q));
+    q.b1 = s.b1;
+    q.b2 = s.b2;
+    q.a1 = s.a1;
+    q.a2 = s.a2;
+    const double a1 = s.a1, a2 = s.a2, b1 = s.b1, b2 = s.b2;
+    const M2 A{0.0, 1.0, a2, a1};
+    const M2 C = mpow(A, static_cast<unsigned long long>(N));
+    const M2 Q = mpow(C, static_cast<unsigned long long>(rows));
+    M2 P = C;
+    for (int t = 0; t < IIR_MAX_ROWS; ++t) {
+        tab[IIR_TAB_CPOW + t] = to_f4(P);
+        P = mmul(P, C);
+    }
+    M2 G = C;
+    if (kind != IIR_KIND_PH) {
+        // Cyclic reduction: A_{k+1}(z) = A_k(z) A_k(-z) in z^(2^k); e_k, f_k are the stride-2^k
+        // recurrence coefficients y[n] + e_k y[n-2^k] + f_k y[n-2^(k+1)] = v_k[n]
+        // (stcr_kernels.cuh:93-125 computes the same chain in float32).
+        const int L = ilog2(N);
+        double e = -a1, f = -a2;
+        q.e0 = static_cast<float>(e);
+        q.f0 = static_cast<float>(f);
+        q.fir5[0] = static_cast<float>(b1 - e);
+        q.fir5[1] = static_cast<float>(b2 - e * b1 + f);
+        q.fir5[2] = static_cast<float>(f * b1 - e * b2);
+        q.fir5[3] = static_cast<float>(f * b2);
+        for (int k = 1; k <= L; ++k) {
+            const double en = 2.0 * f - e * e, fn = f * f;
+            e = en;
+            f = fn;
+            if (k < L) {
+                if (!(std::fabs(e) > 1e-30)) return IIR_ERR_UNSUPPORTED;  // singular elimination
+                q.cr_r[k] = static_cast<float>(f / e);
+                q.cr_e[k] = static_cast<float>(e);
+                q.cr_c[k] = static_cast<float>(e - f / e);
+                q.cr_d[k] = static_cast<float>(-f * f / e);
+            }
+        }
+        q.top_e = static_cast<float>(e);
+        q.top_f = static_cast<float>(f);
+        G = M2{0.0, 1.0, -f, -e};
+    }
+    P = G;
+    for (int t = 0; t < 32; ++t) {
+        tab[IIR_TAB_GPOW + t] = to_f4(P);
+        P = mmul(P, G);
+    }
+    M2 Gk = G;
+    for (int k = 0; k < 6; ++k) {
+        const float4 g = to_f4(Gk);
+        q.M[k][0] = g.x;
+        q.M[k][1] = g.y;
+        q.M[k][2] = g.z;
+        q.M[k][3] = g.w;
+        Gk = mmul(Gk, Gk);
+    }
+    M2 Pq{1, 0, 0, 1};
+    for (int l = 0; l <= 32; ++l) {
+        tab[IIR_TAB_QC + l] = to_f4(Pq);
+        Pq = mmul(Pq, Q);
+    }
+    const M2 Qg = mpow(Q, static_cast<unsigned long long>(IIR_GROUP));
+    Pq = M2{1, 0, 0, 1};
+    for (int l = 0; l <= 32; ++l) {
+        tab[IIR_TAB_QG + l] = to_f4(Pq);
+        Pq = mmul(Pq, Qg);
+    }
+    for (int l = IIR_TAB_QG + 33; l < IIR_TAB_STRIDE; ++l) tab[l] = make_float4(0, 0, 0, 0);
+    return IIR_OK;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda needed).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// 2D tensor map over a float32 signal viewed as 32-float (128-byte) lines, box = one block
+// (lines x 32), 128-byte swizzle. Returns false if the map cannot be built.
+bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int lines_per_block) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || n < 32 || (reinterpret_cast<uintptr_t>(base) & 15u)) return false;
+    const cuuint64_t dims[2] = {32ull, static_cast<cuuint64_t>(n / 32)};
+    const cuuint64_t strides[1] = {128ull};
+    const cuuint32_t box[2] = {32u, static_cast<cuuint32_t>(lines_per_block)};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+int cuda_status(cudaError_t e) {
+    if (e == cudaSuccess) return IIR_OK;
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? IIR_ERR_OUT_OF_MEMORY : IIR_ERR_CUDA;
+}
+
+}  // namespace
+
+// -------------------------------------------------------------------------------------------
+// plan
+// -------------------------------------------------------------------------------------------
+struct iir_plan {
+    int device = 0;
+    int kind = 0;
+    int B = 0, N = 0;          // PLR: threads per block, values per thread
+    int order = 0;             // PLR order
+    int n_sections = 0;
+    int sms = 0;
+    int grid_max = 0;
+    const KernelEntry* entry = nullptr;
+    IirLaunchState* d_state = nullptr;
+    unsigned long long* d_carry = nullptr;
+    size_t carry_cap = 0;      // chunks
+    float4* d_tables = nullptr;
+    float* d_fac = nullptr;    // PLR factor arrays
+    IirParams params{};
+    IirPlrParams plr{};
+    long long timeout_ns = 1000000000ll;
+    long long withhold = -1;
+    unsigned long long launches = 0;  // since the carry slots were last zeroed
+    size_t carry_bytes = 0;
+};
+
+namespace {
+
+int default_geometry(int kind, int n_sections, int& B, int& N) {
+    if (kind == IIR_KIND_PLR) {
+        const int order = 2 * n_sections;
+        if (B <= 0) B = order <= 2 ? 512 : order <= 4 ? 256 : order <= 8 ? 128 : 64;
+        if (N <= 0) N = 8;
+        return IIR_OK;
+    }
+    if (B <= 0) B = 32;
+    if (N <= 0) N = 64;
+    return IIR_OK;
+}
+
+int resolve_auto(int kernel, int n_sections) {
+    if (kernel != IIR_KERNEL_AUTO) return kernel;
+    (void)n_sections;
+    return IIR_KERNEL_PH;
+}
+
+// samples per block (= per lookback unit)
+size_t chunk_samples(const iir_plan* p) {
+    return p->kind == IIR_KIND_PLR ? static_cast<size_t>(p->B) * p->N : static_cast<size_t>(p->entry->rows) * p->N;
+}
+
+// 64-bit words of carry slots per section (chunk slots, then one slot per group of chunks)
+size_t carry_words_per_section(const iir_plan* p, size_t cap_chunks) {
+    if (p->kind == IIR_KIND_PLR) return 2 * static_cast<size_t>(p->order) * cap_chunks;
+    return 4 * (cap_chunks + cap_chunks / IIR_GROUP + 2);
+}
+
+int alloc_carry(iir_plan* p, size_t cap_chunks, cudaStream_t stream) {
+    if (p->d_carry) {
+        cudaStreamSynchronize(stream);
+        cudaFree(p->d_carry);
+        p->d_carry = nullptr;
+    }
+    cap_chunks = std::max<size_t>(cap_chunks, 1);
+    const size_t per_section = carry_words_per_section(p, cap_chunks);
+    const size_t sections = (p->kind == IIR_KIND_PLR) ? 1 : static_cast<size_t>(p->n_sections);
+    const size_t bytes = per_section * sections * sizeof(unsigned long long);
+    int st = cuda_status(cudaMalloc(&p->d_carry, bytes));
+    if (st) return st;
+    // Zeroed once at allocation (reference: cudaMemset(status, 0), src/test_accuracy.cu:145).
+    st = cuda_status(cudaMemset(p->d_carry, 0, bytes));
+    if (st) return st;
+    p->carry_cap = cap_chunks;
+    p->carry_bytes = bytes;
+    return IIR_OK;
+}
+
+int plan_common_alloc(iir_plan* p, size_t max_n) {
+    int st = cuda_status(cudaGetDevice(&p->device));
+    if (st) return st;
+    st = cuda_status(cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, p->device));
+    if (st) return st;
+    const int nb = blocks_per_sm(*p->entry, p->device);
+    if (nb <= 0) return IIR_ERR_UNSUPPORTED;
+    p->grid_max = nb * p->sms;
+    st = cuda_status(cudaMalloc(&p->d_state, sizeof(IirLaunchState)));
+    if (st) return st;
+    st = cuda_status(cudaMemset(p->d_state, 0, sizeof(IirLaunchState)));
+    if (st) return st;
+    const size_t chunk = chunk_samples(p);
+    return alloc_carry(p, (std::max<size_t>(max_n, 1) + chunk - 1) / chunk, nullptr);
+}
+
+void plan_free(iir_plan* p) {
+    if (!p) return;
+    if (p->d_state) cudaFree(p->d_state);
+    if (p->d_carry) cudaFree(p->d_carry);
+    if (p->d_tables) cudaFree(p->d_tables);
+    if (p->d_fac) cudaFree(p->d_fac);
+    delete p;
+}
+
+// PLR: n-nacci factor arrays fac_j[i], the response at offset i of the order-k recurrence
+// to a unit initial condition y[-k+j] = 1 (plr_kernels.cuh:149-409, there in float32).
+void plr_factors(const double* a, int order, int chunk, std::vector<float>& fac) {
+    fac.assign(static_cast<size_t>(order) * chunk, 0.f);
+    std::vector<double> v(static_cast<size_t>(chunk) + order);
+    for (int j = 0; j < order; ++j) {
+        std::fill(v.begin(), v.end(), 0.0);
+        v[j] = 1.0;  // history slot j: y[j - order]
+        for (int i = order; i < chunk + order; ++i) {
+            double acc = 0.0;
+            for (int m = 0; m < order; ++m) acc += a[m] * v[i - 1 - m];
+            v[i] = acc;
+        }
+        for (int i = 0; i < chunk; ++i) fac[static_cast<size_t>(j) * chunk + i] = static_cast<float>(v[i + order]);
+    }
+}
+
+int plan_create_plr(iir_plan** out, const double* b, const double* a, int order, double gain, int B, int X,
+                    size_t max_n) {
+    if (order != 2 && order != 4 && order != 8 && order != 16) return IIR_ERR_UNSUPPORTED;
+    int Bd = B, Xd = X;
+    default_geometry(IIR_KIND_PLR, order / 2, Bd, Xd);
+    const KernelEntry* e = find_entry(IIR_KIND_PLR, Bd, Xd, order);
+    if (!e) return IIR_ERR_UNSUPPORTED;
+    iir_plan* p = new iir_plan();
+    p->kind = IIR_KIND_PLR;
+    p->B = Bd;
+    p->N = Xd;
+    p->order = order;
+    p->n_sections = order / 2;
+    p->entry = e;
+    int st = plan_common_alloc(p, max_n);
+    if (st) {
+        plan_free(p);
+        return st;
+    }
+    const int chunk = Bd * Xd;
+    std::vector<float> fac;
+    plr_factors(a, order, chunk, fac);
+    st = cuda_status(cudaMalloc(&p->d_fac, fac.size() * sizeof(float)));
+    if (!st) st = cuda_status(cudaMemcpy(p->d_fac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (st) {
+        plan_free(p);
+        return st;
+    }
+    IirPlrParams& q = p->plr;
+    std::memset(&q, 0, sizeof(q));
+    q.state = p->d_state;
+    q.fac = p->d_fac;
+    q.chunk = chunk;
+    q.gain = static_cast<float>(gain);
+    for (int j = 0; j < order; ++j) {
+        q.b[j] = static_cast<float>(b[j]);
+        q.a[j] = static_cast<float>(a[j]);
+    }
+    *out = p;
+    return IIR_OK;
+}
+
+// Merges float32 sections into one direct-form polynomial pair (FP64 convolution).
+void merge_sections(const std::vector<SectionF32>& secs, std::vector<double>& bt, std::vector<double>& at) {
+    std::vector<double> bp{1.0}, ap{1.0};
+    for (const SectionF32& s : secs) {
+        const double bs[3] = {1.0, s.b1, s.b2};
+        const double as[3] = {1.0, -static_cast<double>(s.a1), -static_cast<double>(s.a2)};
+        std::vector<double> nb(bp.size() + 2, 0.0), na(ap.size() + 2, 0.0);
+        for (size_t i = 0; i < bp.size(); ++i)
+            for (int j = 0; j < 3; ++j) nb[i + j] += bp[i] * bs[j];
+        for (size_t i = 0; i < ap.size(); ++i)
+            for (int j = 0; j < 3; ++j) na[i + j] += ap[i] * as[j];
+        bp.swap(nb);
+        ap.swap(na);
+    }
+    bt.assign(bp.begin() + 1, bp.end());
+    at.resize(ap.size() - 1);
+    for (size_t i = 1; i < ap.size(); ++i) at[i - 1] = -ap[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+int iir_version(void) { return 10000; }
+
+const char* iir_status_string(int status) {
+    switch (status) {
+        case IIR_OK: return "ok";
+        case IIR_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case IIR_ERR_UNSUPPORTED: return "unsupported realization / geometry / filter";
+        case IIR_ERR_CUDA: return "CUDA runtime error";
+        case IIR_ERR_LOOKBACK_TIMEOUT: return "lookback wait exceeded the plan's limit";
+        case IIR_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case IIR_ERR_TOO_LARGE: return "too many samples";
+        default: return "unknown status";
+    }
+}
+
+int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel, int block_size, int n_blocks,
+                    size_t max_n) {
+    if (!out || !sos) return IIR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_sections < 1 || n_sections > IIR_MAX_SECTIONS) return IIR_ERR_INVALID_ARGUMENT;
+    kernel = resolve_auto(kernel, n_sections);
+    if (kernel < IIR_KERNEL_PH || kernel > IIR_KERNEL_PLR) return IIR_ERR_INVALID_ARGUMENT;
+    std::vector<SectionF32> secs;
+    double gain = 1.0;
+    int st = normalise_sos(sos, n_sections, secs, gain);
+    if (st) return st;
+    if (kernel == IIR_KERNEL_PLR) {
+        std::vector<double> bt, at;
+        merge_sections(secs, bt, at);
+        return plan_create_plr(out, bt.data(), at.data(), 2 * n_sections, gain, block_size, n_blocks, max_n);
+    }
+    int B = block_size, N = n_blocks;
+    default_geometry(kernel, n_sections, B, N);
+    const KernelEntry* e = find_entry(kernel, B, N, 0);
+    if (!e) return IIR_ERR_UNSUPPORTED;
+    iir_plan* p = new iir_plan();
+    p->kind = kernel;
+    p->B = B;
+    p->N = N;
+    p->n_sections = n_sections;
+    p->entry = e;
+    IirParams& q = p->params;
+    std::memset(&q, 0, sizeof(q));
+    std::vector<float4> tabs(static_cast<size_t>(n_sections) * IIR_TAB_STRIDE);
+    for (int s = 0; s < n_sections; ++s) {
+        st = precompute_section(secs[s], kernel, e->rows, N, q.sec[s], tabs.data() + static_cast<size_t>(s) * IIR_TAB_STRIDE);
+        if (st) {
+            delete p;
+            return st;
+        }
+    }
+    st = plan_common_alloc(p, max_n);
+    if (!st) st = cuda_status(cudaMalloc(&p->d_tables, tabs.size() * sizeof(float4)));
+    if (!st)
+        st = cuda_status(cudaMemcpy(p->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (st) {
+        plan_free(p);
+        return st;
+    }
+    q.state = p->d_state;
+    q.tables = p->d_tables;
+    q.n_sections = n_sections;
+    q.gain = static_cast<float>(gain);
+    *out = p;
+    return IIR_OK;
+}
+
+int iir_plan_create_plr_ba(iir_plan** out, const double* b, const double* a, int order, double gain, int block_size,
+                           int values_per_thread, size_t max_n) {
+    if (!out || !b || !a) return IIR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return plan_create_plr(out, b, a, order, gain, block_size, values_per_thread, max_n);
+}
+
+int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stream_) {
+    if (!p || (n > 0 && (!x || !y))) return IIR_ERR_INVALID_ARGUMENT;
+    if (n == 0) return IIR_OK;
+    if (n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
+    const char* xb = reinterpret_cast<const char*>(x);
+    const char* yb = reinterpret_cast<const char*>(y);
+    if (xb < yb + n * sizeof(float) && yb < xb + n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;  // overlap
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    const size_t chunk = chunk_samples(p);
+    const size_t nchunks = (n + chunk - 1) / chunk;
+    if (nchunks > 0xffffffffull) return IIR_ERR_TOO_LARGE;
+    if (nchunks > p->carry_cap) {
+        const int st = alloc_carry(p, nchunks, stream);
+        if (st) return st;
+    }
+    // one block per chunk (blocks take tickets in start order; no residency assumption)
+    if (nchunks > 0x7fffffffull) return IIR_ERR_TOO_LARGE;
+    const int grid = static_cast<int>(nchunks);
+    // Flags are 32-bit functions of the launch epoch: re-zero the slots and the launch state
+    // long before the epoch could wrap (the reference zeroes its status buffer once).
+    if (++p->launches >= (1ull << 30)) {
+        int st = cuda_status(cudaMemsetAsync(p->d_carry, 0, p->carry_bytes, stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(p->d_state, 0, sizeof(IirLaunchState), stream));
+        if (st) return st;
+        p->launches = 1;
+    }
+    const bool aligned = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15u) == 0;
+    cudaError_t err;
+    if (p->kind == IIR_KIND_PLR) {
+        IirPlrParams& q = p->plr;
+        q.x = x;
+        q.y = y;
+        q.n = static_cast<long long>(n);
+        q.carry = p->d_carry;
+        q.nchunks = static_cast<unsigned int>(nchunks);
+        q.carry_cap = static_cast<unsigned int>(p->carry_cap);
+        q.timeout_ns = p->timeout_ns;
+        q.withhold_chunk = p->withhold;
+        void* args[] = {&q};
+        err = cudaLaunchKernel(p->entry->fn, dim3(grid), dim3(p->entry->threads), args, p->entry->smem, stream);
+    } else {
+        IirParams& q = p->params;
+        q.x = x;
+        q.y = y;
+        q.n = static_cast<long long>(n);
+        q.carry = p->d_carry;
+        q.nchunks = static_cast<unsigned int>(nchunks);
+        q.carry_cap = static_cast<unsigned int>(p->carry_cap);
+        q.carry_stride = carry_words_per_section(p, p->carry_cap);
+        const int lines = static_cast<int>(chunk / 32);
+        q.use_tma = (aligned && encode_lines_map(&q.tmap_x, x, static_cast<long long>(n), lines) &&
+                     encode_lines_map(&q.tmap_y, y, static_cast<long long>(n), lines))
+                        ? 1
+                        : 0;
+        q.timeout_ns = p->timeout_ns;
+        q.withhold_chunk = p->withhold;
+        void* args[] = {&q};
+        err = cudaLaunchKernel(p->entry->fn, dim3(grid), dim3(p->entry->threads), args, p->entry->smem, stream);
+    }
+    p->withhold = -1;  // one launch only
+    return cuda_status(err);
+}
+
+int iir_plan_check(iir_plan* p, void* stream_) {
+    if (!p) return IIR_ERR_INVALID_ARGUMENT;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    int st = cuda_status(cudaStreamSynchronize(stream));
+    if (st) return st;
+    IirLaunchState hs;
+    st = cuda_status(cudaMemcpy(&hs, p->d_state, sizeof(hs), cudaMemcpyDeviceToHost));
+    if (st) return st;
+    if (hs.error == 0ull) return IIR_OK;
+    const unsigned long long zero = 0ull;
+    cudaMemcpy(reinterpret_cast<char*>(p->d_state) + offsetof(IirLaunchState, error), &zero, sizeof(zero),
+               cudaMemcpyHostToDevice);
+    const unsigned code = static_cast<unsigned>(hs.error & 0xffffffffull);
+    return code == IIR_DEV_ERR_TIMEOUT ? IIR_ERR_LOOKBACK_TIMEOUT : IIR_ERR_CUDA;
+}
+
+int iir_plan_set_timeout_ns(iir_plan* p, long long timeout_ns) {
+    if (!p || timeout_ns <= 0) return IIR_ERR_INVALID_ARGUMENT;
+    p->timeout_ns = timeout_ns;
+    return IIR_OK;
+}
+
+int iir_plan_debug_withhold(iir_plan* p, long long chunk) {
+    if (!p) return IIR_ERR_INVALID_ARGUMENT;
+    p->withhold = chunk;
+    return IIR_OK;
+}
+
+int iir_plan_info(const iir_plan* p, int* kernel, int* block_size, int* n_blocks, int* grid, int* n_sections) {
+    if (!p) return IIR_ERR_INVALID_ARGUMENT;
+    if (kernel) *kernel = p->kind;
+    if (block_size) *block_size = p->B;
+    if (n_blocks) *n_blocks = p->N;
+    if (grid) *grid = p->grid_max;
+    if (n_sections) *n_sections = p->n_sections;
+    return IIR_OK;
+}
+
+int iir_plan_launches_per_execute(const iir_plan* p) { return p ? 1 : 0; }
+
+#ifdef IIR_PROFILE
+int iir_plan_debug_profile(iir_plan* p, void* dev_buffer) {
+    if (!p) return IIR_ERR_INVALID_ARGUMENT;
+    p->params.prof = static_cast<unsigned long long*>(dev_buffer);
+    return IIR_OK;
+}
+#endif
+
+int iir_plan_destroy(iir_plan* p) {
+    if (!p) return IIR_ERR_INVALID_ARGUMENT;
+    plan_free(p);
+    return IIR_OK;
+}
+
+}  // extern "C"
+
+// -------------------------------------------------------------------------------------------
+// one-shot API with a plan cache keyed by (device, stream, kernel, geometry, filter bytes)
+// -------------------------------------------------------------------------------------------
+namespace {
+struct CacheKey {
+    int device;
+    void* stream;
+    int kernel, B, N, n_sections;
+    std::string sos;
+    bool operator<(const CacheKey& o) const {
+        return std::tie(device, stream, kernel, B, N, n_sections, sos) <
+               std::tie(o.device, o.stream, o.kernel, o.B, o.N, o.n_sections, o.sos);
+    }
+};
+std::mutex& cache_mu() {
+    static std::mutex m;
+    return m;
+}
+std::map<CacheKey, iir_plan*>& cache() {
+    static std::map<CacheKey, iir_plan*> c;
+    return c;
+}
+}  // namespace
+
+extern "C" int iir_sos_filter_geom(const float* x, float* y, size_t n, const float* sos, int n_sections, int kernel,
+                                   int block_size, int n_blocks, void* stream) {
+    if (!sos || n_sections < 1 || n_sections > IIR_MAX_SECTIONS) return IIR_ERR_INVALID_ARGUMENT;
+    int device = 0;
+    int st = cuda_status(cudaGetDevice(&device));
+    if (st) return st;
+    CacheKey key{device, stream, kernel, block_size, n_blocks, n_sections,
+                 std::string(reinterpret_cast<const char*>(sos), sizeof(float) * 6 * n_sections)};
+    std::lock_guard<std::mutex> lk(cache_mu());
+    auto it = cache().find(key);
+    iir_plan* p = nullptr;
+    if (it == cache().end()) {
+        st = iir_plan_create(&p, sos, n_sections, kernel, block_size, n_blocks, n);
+        if (st) return st;
+        cache()[key] = p;
+    } else {
+        p = it->second;
+    }
+    return iir_plan_execute(p, x, y, n, stream);
+}
+
+extern "C" int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_sections, int kernel,
+                              void* stream) {
+    return iir_sos_filter_geom(x, y, n, sos, n_sections, kernel, 0, 0, stream);
+}
+
+extern "C" int iir_cache_clear(void) {
+    std::lock_guard<std::mutex> lk(cache_mu());
+    cudaDeviceSynchronize();
+    for (auto& kv : cache()) plan_free(kv.second);
+    cache().clear();
+    return IIR_OK;
+}

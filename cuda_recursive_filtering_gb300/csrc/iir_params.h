@@ -1,0 +1,98 @@
+// iir_params.h — launch parameters shared by the host planner and the sm_103a kernels.
+//
+// The reference keeps every per-filter constant in module-global __constant__ /
+// __device__ symbols filled by cudaMemcpyToSymbol (include/ph_kernels.cuh:45-49,186-199),
+// so one module holds one filter. Here the warp-uniform constants travel in a
+// __grid_constant__ parameter block (constant bank, free FMA operands) and the
+// lane-indexed tables live in a plan-owned device buffer, so any number of plans coexist.
+#pragma once
+#include <cuda.h>
+#include <stdint.h>
+
+#define IIR_MAX_SECTIONS 8
+#define IIR_MAX_LEVELS 8          // log2(N_BLOCKS) <= 7
+#define IIR_MAX_ROWS 256          // rows (threads x 1 row) per block for the row-major realizations
+#define IIR_PLR_MAX_ORDER 16
+
+// Lane tables per section, in float4 units (row-major 2x2 matrices {m00, m01, m10, m11}):
+//   [TAB_CPOW + r] = C^(r+1),  C = A^N   (pair transition over one row), r < rows per chunk
+//   [TAB_GPOW + t] = G^(t+1),  G = row-scan companion (C for PH; top-level cyclic-reduction
+//                                 companion for STCR / DTCR), t < 32 rows per warp
+//   [TAB_QC + l]   = Q^l,      Q = A^(rows*N) (chunk transition), l <= 32
+//   [TAB_QG + l]   = Q^(32 l)  (group transition powers), l <= 32
+#define IIR_GROUP 32
+#define IIR_TAB_CPOW 0
+#define IIR_TAB_GPOW 256
+#define IIR_TAB_QC 288
+#define IIR_TAB_QG 321
+#define IIR_TAB_STRIDE 356
+
+// Device-side per-plan launch state. `ticket` packs the launch epoch (the reference's
+// `launch` index: part_flag = 2*launch+1, full_flag = 2*launch+2; ph_kernels.cuh:16-24) in its
+// high 32 bits and the chunk ticket of the current launch in its low 32 bits, so one atomic
+// gives a block both. The block that draws the last chunk of a launch resets the ticket and
+// advances the epoch for the next launch (no per-block exit atomics; graph replays and
+// launches of different sizes stay consistent). Chunk order = ticket order = block start
+// order (the forward-progress argument of ph_kernels.cuh:227-229).
+struct IirLaunchState {
+    unsigned long long ticket;       // (epoch << 32) | ticket
+    unsigned long long error;        // (epoch << 32) | status code of the first failure
+    unsigned long long pad[2];
+};
+
+struct IirSection {
+    float b1, b2;           // FIR taps after b0 normalisation (b0 = 1)
+    float a1, a2;           // recurrence y[n] = w[n] + a1 y[n-1] + a2 y[n-2]
+    float M[6][4];          // row-scan round matrices G^(2^k), k = 0..5
+    // cyclic-reduction factors (STCR / DTCR), level k = 1..7 at index k:
+    //   r_k = f_k / e_k, e_k, c_k = e_k - f_k/e_k, d_k = -f_k^2 / e_k
+    float cr_r[IIR_MAX_LEVELS], cr_e[IIR_MAX_LEVELS], cr_c[IIR_MAX_LEVELS], cr_d[IIR_MAX_LEVELS];
+    float e0, f0;           // e_0 = -a1, f_0 = -a2 (first double-sided round)
+    float fir5[4];          // fused FIR + first CR round taps D1..D4 (DTCR)
+    float top_e, top_f;     // top-level recurrence across rows: Y_t + e_L Y_{t-1} + f_L Y_{t-2}
+    float pad[2];
+};
+
+struct IirParams {
+    CUtensorMap tmap_x;               // 2D view of x as 32-float lines, 128B swizzle (bulk path)
+    CUtensorMap tmap_y;
+    const float* x;
+    float* y;
+    long long n;
+    unsigned long long* carry;        // per section: [carry_cap][4] chunk slots, then group slots
+    IirLaunchState* state;
+    const float4* tables;             // [n_sections][IIR_TAB_STRIDE]
+    unsigned long long carry_stride;  // words per section
+    long long timeout_ns;             // lookback wait limit
+    long long withhold_chunk;         // fault injection (-1 = off)
+    unsigned int nchunks;
+    unsigned int carry_cap;
+    int n_sections;
+    int use_tma;                      // tensor maps valid (x, y 16-byte aligned) -> TMA staging
+    float gain;
+    int pad0;
+    unsigned long long* prof;         // per-block phase timestamps (IIR_PROFILE builds only)
+    IirSection sec[IIR_MAX_SECTIONS];
+};
+
+// PLR (direct form, order k = 2K) parameters.
+struct IirPlrParams {
+    const float* x;
+    float* y;
+    long long n;
+    unsigned long long* carry;        // [carry_cap][2][k] flag|value words (part, full)
+    IirLaunchState* state;
+    const float* fac;                 // [k][chunk] n-nacci factor arrays (fac[j][i])
+    long long timeout_ns;
+    long long withhold_chunk;
+    unsigned int nchunks;
+    unsigned int carry_cap;
+    int chunk;                        // BLOCK * X
+    float gain;
+    float b[IIR_PLR_MAX_ORDER];       // FIR taps past b0 = 1
+    float a[IIR_PLR_MAX_ORDER];       // recurrence taps: y[n] += a[j] y[n-j-1]
+};
+
+// Status codes stored in IirLaunchState::error (same values as the C ABI).
+#define IIR_DEV_ERR_TIMEOUT 4u
+#define IIR_DEV_ERR_MBARRIER 7u

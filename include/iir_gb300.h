@@ -1,0 +1,130 @@
+/*
+ * iir_gb300.h — C ABI of the GB300 (sm_103a) cascaded-biquad IIR filtering library.
+ *
+ * The reference library (Haotian-RA/cuda_recursive_filtering) is header-only: a
+ * translation unit defines N_SECTIONS / BLOCK_SIZE / N_BLOCKS as macros, calls
+ *   setup_kernel_coefficients(const std::vector<std::array<float,6>>& sos)
+ * (include/ph_kernels.cuh:151, include/stcr_kernels.cuh:191,
+ *  include/dtcr_kernels.cuh:203, include/plr_kernels.cuh:416)
+ * and launches
+ *   KERNEL_FUNC<<<grid, block>>>(in, out, status, partcarry, fullcarry, launch)
+ * (src/test_accuracy.cu:146, src/test_performance.cu:383) on buffers the caller
+ * allocated (src/test_accuracy.cu:136-140).
+ *
+ * This header replaces that surface with run-time arguments:
+ *   - the realization (PH / STCR / DTCR / PLR) and the BLOCK_SIZE x N_BLOCKS
+ *     geometry are arguments, not macros;
+ *   - a plan owns the launch-versioned status/carry buffers (zeroed once at
+ *     allocation, never reset between launches), the monotone launch index and
+ *     the chunk ticket counter, so callers no longer allocate them;
+ *   - every entry point returns an int status code instead of asserting.
+ *
+ * All pointers passed as x / y are DEVICE pointers to float32 samples. Streams are
+ * passed as `void*` holding a cudaStream_t (NULL = legacy default stream).
+ * A plan must be driven from one stream at a time (launches that share a plan's
+ * status buffer must be serialised, as in include/ph_kernels.cuh:26-29).
+ */
+#ifndef IIR_GB300_H
+#define IIR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define IIR_OK                    0
+#define IIR_ERR_INVALID_ARGUMENT (-1)  /* null pointer, bad n_sections, a0 == 0, ...     */
+#define IIR_ERR_UNSUPPORTED      (-2)  /* geometry / order combination not built          */
+#define IIR_ERR_CUDA             (-3)  /* a CUDA runtime call failed                      */
+#define IIR_ERR_LOOKBACK_TIMEOUT (-4)  /* a chunk waited longer than the plan's limit for a
+                                          predecessor's carry; output of that launch is void */
+#define IIR_ERR_OUT_OF_MEMORY    (-5)
+#define IIR_ERR_TOO_LARGE        (-6)  /* n above the plan's capacity / 2^40 samples        */
+
+/* ---- realizations (reference: include/{ph,stcr,dtcr,plr}_kernels.cuh) ----------- */
+#define IIR_KERNEL_AUTO         0   /* fastest realization for the order (tuned on GB300) */
+#define IIR_KERNEL_PH           1   /* PH_32 / PH_64                      ph_kernels.cuh:208,501   */
+#define IIR_KERNEL_STCR         2   /* STCR_*_LOOP (loop-form back-sub)   stcr_kernels.cuh:279,2586 */
+#define IIR_KERNEL_STCR_UNROLL  3   /* STCR_*_UNROLL_* (register form)    stcr_kernels.cuh:608-3605 */
+#define IIR_KERNEL_DTCR         4   /* DTCR_*_LOOP                        dtcr_kernels.cuh:291,2500 */
+#define IIR_KERNEL_DTCR_UNROLL  5   /* DTCR_*_UNROLL_*                    dtcr_kernels.cuh:660-3521 */
+#define IIR_KERNEL_PLR          6   /* PLR_2/4/8/16 direct form           plr_kernels.cuh:484-3107  */
+
+typedef struct iir_plan iir_plan;
+
+/*
+ * One-shot filtering, the drop-in for "setup_kernel_coefficients(sos) + one launch".
+ *   sos        : n_sections rows of {b0, b1, b2, a0, a1, a2} (host memory, scipy layout).
+ *                Rows are normalised on the host in FP64 (b0 = a0 = 1); the removed gain
+ *                prod(b0/a0) is applied to the input, as the reference's drivers apply
+ *                FILTER_GAIN (src/test_accuracy.cu:120-124). Already-normalised rows
+ *                (b0 = a0 = 1, the reference's convention, ph_kernels.cuh:157-161) pass through
+ *                unchanged.
+ *   kernel     : IIR_KERNEL_*; block_size/n_blocks = 0 selects the tuned geometry.
+ *   x, y       : device float32 arrays of n samples; they must not overlap.
+ *   stream     : cudaStream_t. The call is stream-ordered; plans are cached internally
+ *                per (device, stream, filter, kernel, geometry).
+ * Zero initial state, as the reference (xi1/xi2/yi1/yi2 = 0, ph_kernels.cuh:162-165).
+ */
+int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_sections,
+                   int kernel, void* stream);
+
+/* Same as iir_sos_filter with an explicit BLOCK_SIZE x N_BLOCKS geometry
+ * (reference: -DBLOCK_SIZE / -DN_BLOCKS, run_performance.sh:22-60). For PLR, block_size is
+ * the thread-block size and n_blocks the values per thread (PLR_X, plr_kernels.cuh:94-101). */
+int iir_sos_filter_geom(const float* x, float* y, size_t n, const float* sos, int n_sections,
+                        int kernel, int block_size, int n_blocks, void* stream);
+
+/* ---- plan API (reference: setup_kernel_coefficients + the caller-owned buffers) ---- */
+
+/* Creates a plan on the current CUDA device. The status/carry buffers are sized for
+ * max_n samples and zeroed once here (reference contract, ph_kernels.cuh:16-24). */
+int iir_plan_create(iir_plan** plan, const float* sos, int n_sections, int kernel,
+                    int block_size, int n_blocks, size_t max_n);
+
+/* PLR from direct-form taps (reference: PLR_FILTER_B / PLR_FILTER_A of filter_taps.hpp,
+ * plr_kernels.cuh:416-427). b[order], a[order] are the taps past the implicit b0 = 1 and
+ * the recurrence taps with the sign convention y[n] += a[j] * y[n-j-1]; `gain` multiplies
+ * the input. order must be 2, 4, 8 or 16. */
+int iir_plan_create_plr_ba(iir_plan** plan, const double* b, const double* a, int order,
+                           double gain, int block_size, int values_per_thread, size_t max_n);
+
+/* Launches the filter on x[0..n) -> y[0..n) on `stream` (stream-ordered, no sync). */
+int iir_plan_execute(iir_plan* plan, const float* x, float* y, size_t n, void* stream);
+
+/* Synchronises `stream`, returns the first device-side error recorded by a launch of this
+ * plan since the previous call (IIR_OK if none) and clears it. */
+int iir_plan_check(iir_plan* plan, void* stream);
+
+/* Sets the lookback wait limit in nanoseconds (default 1e9). A chunk that waits longer
+ * for a predecessor's carry records IIR_ERR_LOOKBACK_TIMEOUT and every block of that
+ * launch returns early. */
+int iir_plan_set_timeout_ns(iir_plan* plan, long long timeout_ns);
+
+/* Fault injection for tests of the bounded wait: chunk `chunk` of the NEXT launch skips
+ * publishing its carries (so its successors' waits run out). -1 disables. */
+int iir_plan_debug_withhold(iir_plan* plan, long long chunk);
+
+/* Resolved realization / geometry of a plan (after IIR_KERNEL_AUTO and defaults). */
+int iir_plan_info(const iir_plan* plan, int* kernel, int* block_size, int* n_blocks,
+                  int* grid, int* n_sections);
+
+/* Number of kernel launches one iir_plan_execute issues (for launch accounting). */
+int iir_plan_launches_per_execute(const iir_plan* plan);
+
+int iir_plan_destroy(iir_plan* plan);
+
+/* ---- helpers ------------------------------------------------------------------------- */
+const char* iir_status_string(int status);
+int iir_version(void);          /* major*10000 + minor*100 + patch */
+
+/* Drops every plan cached by iir_sos_filter (frees their device memory). */
+int iir_cache_clear(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IIR_GB300_H */

@@ -1,0 +1,150 @@
+"""GPU parity: every realization x geometry x order against the FP64 oracle (pinned to the
+reference's reference.bin) and against the reference's float32 emulator outputs, through the
+C ABI. Tolerances (written per test): the reference's gate max|err| <= 1e-4 * max|ref|
+(src/test_accuracy.cu:178-188) everywhere it applies, and the benchmark spec's bound
+max|err| / RMS(ref) <= 1e-5 at orders 2-8 (2e-5 at order 16) for the cascaded realizations.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import GOLDEN
+from cuda_recursive_filtering_gb300 import Plan, formats, sosfilt
+
+pytestmark = pytest.mark.gpu
+
+CASCADED = ["PH", "STCR", "STCR_UNROLL", "DTCR", "DTCR_UNROLL"]
+GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
+ORDERS = (2, 4, 8, 16)
+RMS_TOL = {2: 1e-5, 4: 1e-5, 8: 1e-5, 16: 2e-5}
+
+
+def butter(order, cutoff=0.1):
+    from scipy import signal
+    return signal.butter(order, cutoff, output="sos")
+
+
+def run_plan(plan, x_np):
+    x = torch.from_numpy(np.ascontiguousarray(x_np, np.float32)).cuda()
+    y = plan(x)
+    plan.check()
+    return y.cpu().numpy()
+
+
+def golden(sos, x):
+    xd, ref = oracle.reference_golden(sos, x)
+    return ref
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+@pytest.mark.parametrize("geom", GEOMS, ids=lambda g: f"{g[0]}x{g[1]}")
+@pytest.mark.parametrize("order", ORDERS)
+def test_cascaded_vs_oracle(kernel, geom, order, cuda_device):
+    sos = butter(order)
+    n = 37 * geom[0] * geom[1] + 123  # many chunks + a ragged last chunk
+    x = np.random.default_rng(order).uniform(-1, 1, n).astype(np.float32)
+    plan = Plan(sos, kernel, *geom, max_n=n)
+    y = run_plan(plan, x)
+    e = oracle.errors(y, golden(sos, x))
+    assert e["finite"]
+    assert e["rel_max"] <= 1e-4, e
+    assert e["rel_rms"] <= RMS_TOL[order], e
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+@pytest.mark.parametrize("order", ORDERS)
+def test_reference_bin_fixture(kernel, order, cuda_device):
+    """The reference's own test: its filter_taps.hpp + input formula vs its reference.bin."""
+    d = os.path.join(GOLDEN, f"ref_order{order}")
+    taps = formats.parse_filter_taps(os.path.join(d, "filter_taps.hpp"))
+    ref = formats.read_reference_bin(os.path.join(d, "reference.bin"))
+    x = formats.reference_input(ref.size, taps["gain"])
+    for geom in ((32, 32), (32, 64)):
+        y = run_plan(Plan(taps["sos"], kernel, *geom, max_n=ref.size), x)
+        e = oracle.errors(y, ref)
+        assert e["rel_max"] <= 1e-4, (geom, e)  # src/test_accuracy.cu:178
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+@pytest.mark.parametrize("order", ORDERS)
+@pytest.mark.parametrize("geom", GEOMS, ids=lambda g: f"{g[0]}x{g[1]}")
+def test_matches_reference_emulators(kernel, order, geom, cuda_device):
+    """Same input as the reference's STCR/DTCR float32 emulators (3 chunks): our float32 output
+    agrees with theirs to the reference's gate, and both sit at float32 round-off of FP64."""
+    emu = np.load(os.path.join(GOLDEN, "emulators.npz"))
+    tag = f"{order}_{geom[0]}x{geom[1]}"
+    xd = emu[f"x_dtcr_{tag}"]  # gain already applied
+    sos = emu[f"sos_{order}"]  # b0-normalised float32
+    y = run_plan(Plan(sos, kernel, *geom, max_n=xd.size), xd)
+    ref = emu[f"ref_stcr_{tag}"]
+    for name in ("stcr", "dtcr"):
+        other = emu[f"{name}_{tag}"]
+        assert np.max(np.abs(y.astype(np.float64) - other)) <= 1e-5 * np.max(np.abs(ref)), name
+    assert oracle.errors(y, ref)["rel_max"] <= 2e-6
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+def test_edge_sizes(kernel, cuda_device):
+    sos = butter(4)
+    plan = Plan(sos, kernel, 32, 64, max_n=1 << 14)
+    for n in (1, 2, 3, 5, 64, 2047, 2048, 2049, 4096 + 7):
+        x = np.random.default_rng(n).uniform(-1, 1, n).astype(np.float32)
+        y = run_plan(plan, x)
+        e = oracle.errors(y, golden(sos, x))
+        assert e["rel_max"] <= 1e-4, (n, e)
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+def test_repeated_launches_and_growth(kernel, cuda_device):
+    """Launch-versioned flags: the status buffer is never reset; sizes vary between launches
+    and the carry buffer grows past max_n."""
+    sos = butter(8)
+    plan = Plan(sos, kernel, 32, 32, max_n=4096)
+    for i, n in enumerate([4096, 100000, 1024, 300000, 4096, 65536]):
+        x = np.random.default_rng(i).uniform(-1, 1, n).astype(np.float32)
+        e = oracle.errors(run_plan(plan, x), golden(sos, x))
+        assert e["rel_max"] <= 1e-4, (i, n, e)
+
+
+@pytest.mark.parametrize("kernel", CASCADED)
+def test_unaligned_buffers(kernel, cuda_device):
+    """Pointers that are not 16-byte aligned use element-wise staging instead of bulk copies."""
+    sos = butter(2)
+    n = 50000
+    x = np.random.default_rng(5).uniform(-1, 1, n + 1).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.zeros(n + 3, device="cuda")
+    plan = Plan(sos, kernel, 32, 64, max_n=n)
+    plan(xt[1:], out=yt[3:])
+    plan.check()
+    e = oracle.errors(yt[3:].cpu().numpy(), golden(sos, x[1:]))
+    assert e["rel_max"] <= 1e-4
+
+
+def test_one_shot_api_and_raw_sos(cuda_device):
+    """iir_sos_filter takes raw scipy SOS (b0 != 1) and normalises it; cached plans reused."""
+    sos = butter(8, 0.05)
+    x = np.random.default_rng(9).uniform(-1, 1, 1 << 16).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    for kernel in ("AUTO", "PH"):
+        y = sosfilt(sos, xt, kernel=kernel)
+        y2 = sosfilt(sos, xt, kernel=kernel)
+        torch.cuda.synchronize()
+        e = oracle.errors(y.cpu().numpy(), golden(sos, x))
+        assert e["rel_max"] <= 1e-4
+        assert torch.equal(y, y2) or oracle.errors(y2.cpu().numpy(), golden(sos, x))["rel_max"] <= 1e-4
+
+
+def test_config1_order2(cuda_device):
+    """BASELINE config 1: butter(2, 0.1), 2^16 uniform samples (seed 0), PH and DTCR,
+    gate max|err|/RMS <= 1e-5 against FP64 sosfilt."""
+    from cuda_recursive_filtering_gb300 import workloads
+    sos, xt = workloads.plain_order2_small()
+    x = xt.cpu().numpy()
+    ref = golden(sos, x)
+    for kernel in ("PH", "DTCR"):
+        e = oracle.errors(sosfilt(sos, xt, kernel=kernel).cpu().numpy(), ref)
+        assert e["rel_rms"] <= 1e-5, (kernel, e)
