@@ -1,0 +1,302 @@
+// iir_cr.cuh — cyclic-reduction row solver shared by the STCR and DTCR realizations.
+//
+// Reference algorithm (include/stcr_kernels.cuh:279-605, include/dtcr_kernels.cuh:291-657,
+// factors stcr_kernels.cuh:93-147), restated. For the section recurrence
+//     y[n] + e y[n-1] + f y[n-2] = w[n],   e = -a1, f = -a2,  w = FIR(x),
+// one double-sided round multiplies by (1 - e z^-1 + f z^-2):
+//     y[n] + e1 y[n-2] + f1 y[n-4] = v1[n],  v1 = w[n] - e w[n-1] + f w[n-2],
+// which decouples the even and odd samples (DTCR runs the two halves on two threads of a
+// row; STCR runs both halves in one thread). Each half of M = N/2 samples (half index m,
+// row position 2m + p) is then reduced by L-1 levels (L = log2 N); level k has half-stride
+// h = 2^(k-1) and coefficients (e_k, f_k) of the stride-2^k recurrence. In every group of
+// 2h half positions, the dropped position d = g + h - 1 keeps
+//     u[d] = v[d] - (f_k / e_k) v[d - h]
+// and the kept position q = d + h becomes  v'[q] = v[q] - e_k u[d]
+// (the LU-split elimination; v[d - h] is the previous group's kept value before this level,
+// and for the first group the previous row's). After the last level the half's last sample
+// (row position N-2+p) obeys the cross-row recurrence Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t
+// (the reference's "block filtering", here a Kogge-Stone scan per parity). Back-substitution
+// then recovers the dropped positions level by level:
+//     y[d] = u[d] - c_k y[d - h] - d_k y[d - 3h],   c_k = e_k - f_k/e_k,  d_k = -f_k^2/e_k.
+// All of this runs in the zero-padded chunk (zero state before the chunk); the response to
+// the chunk's incoming state is added afterwards (PH-style correction), which keeps the
+// chunk-boundary algebra simple (the reference folds it into the back-substitution with
+// the h/g/p/q factors, stcr_kernels.cuh:479-585).
+//
+// UNROLL selects the register form (literal indices; the reference's hand-unrolled kernels)
+// or the loop form (run-time loops over a thread-local array; the reference's *_LOOP
+// kernels). Both execute the same operations in the same order, so they are bit-identical.
+#pragma once
+#include "iir_device.cuh"
+
+namespace iirgb {
+
+// Exchange area for cross-row values, double buffered per level: [2][ROWS][2 parities].
+template <int ROWS>
+struct CrExchange {
+    float v[2][ROWS][2];
+};
+
+// One parity half of a row. u[] holds the half's values (half index m).
+template <int M, bool UNROLL>
+struct CrHalf {
+    static constexpr int L1 = (M == 8) ? 3 : (M == 16) ? 4 : (M == 32) ? 5 : (M == 64) ? 6 : 0;  // log2(M)
+    static_assert(L1 > 0, "half length");
+
+    // Elimination level k (half-stride h), prev = previous row's kept tail before this level.
+    __device__ __forceinline__ static void eliminate(float (&u)[M], int h, float rk, float ek, float prev) {
+        float old = prev;  // level-(k-1) value of the previous group's kept position
+#pragma unroll(UNROLL ? 64 : 1)
+        for (int g = 0; g < M; g += 2 * h) {
+            const int d = g + h - 1, q = d + h;
+            const float ud = fmaf(-rk, old, u[d]);
+            const float vq = u[q];
+            u[d] = ud;
+            u[q] = fmaf(-ek, ud, vq);
+            old = vq;
+        }
+    }
+    // Back-substitution level k: ym1 = y at half position -1 (previous row's tail),
+    // yfar = y at half position -1 - 2h (previous row's, or two rows back for h = M/2).
+    __device__ __forceinline__ static void backsub(float (&u)[M], int h, float ck, float dk, float ym1, float yfar) {
+#pragma unroll(UNROLL ? 64 : 1)
+        for (int g = 0; g < M; g += 2 * h) {
+            const int d = g + h - 1;
+            const float a1 = u[g > 0 ? g - 1 : 0];
+            const float a3 = u[g >= 4 * h ? g - 1 - 2 * h : 0];
+            const float y1 = (g == 0) ? ym1 : a1;
+            const float y3 = (g == 0) ? yfar : ((g == 2 * h) ? ym1 : a3);
+            u[d] = fmaf(-dk, y3, fmaf(-ck, y1, u[d]));
+        }
+    }
+};
+
+}  // namespace iirgb
+
+namespace iirgb {
+
+constexpr int ilog2_c(int v) { return v <= 1 ? 0 : 1 + ilog2_c(v / 2); }
+
+// STCR (SPLIT = false): one thread per row holds both parity halves.
+// DTCR (SPLIT = true): the two halves of a row run on two neighbouring lanes (dim3(B, 2) in
+// the reference, dtcr_kernels.cuh:56), interleaved so a row's pair shares a warp.
+template <bool SPLIT, int B_, int N_, int ROWS_, bool UNROLL>
+struct CrBlock {
+    static constexpr int B = B_, N = N_, ROWS = ROWS_, M = N_ / 2, L = ilog2_c(N_);
+    static constexpr int TPR = SPLIT ? 2 : 1;   // threads per row
+    static constexpr int NPAR = SPLIT ? 1 : 2;  // parity halves per thread
+    static constexpr int RW = 32 / TPR;         // rows per warp
+    static constexpr int NW = ROWS * TPR / 32;  // row warps
+    static constexpr int THREADS = 32 + NW * 32;
+    static_assert(ROWS % RW == 0 && NW <= 16 && ROWS <= IIR_MAX_ROWS, "rows per chunk");
+    using Half = CrHalf<M, UNROLL>;
+
+    struct Smem {
+        CrExchange<ROWS> xch;
+    };
+    static constexpr size_t SMEM_BYTES = BlockGeom<ROWS, N>::SMEM_BYTES + sizeof(Smem);
+
+    __device__ static Smem* extra(unsigned char* smem) {
+        return reinterpret_cast<Smem*>(block_aux<ROWS, N>(smem) + 1);
+    }
+
+    __device__ static void run(const IirParams& p, unsigned char* smem) {
+        float* buf = chunk_buffer<ROWS, N>(smem);
+        BlockAux* aux = block_aux<ROWS, N>(smem);
+        Smem* ex = extra(smem);
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (warp == 0) block_begin<ROWS, N>(p, buf, aux);
+        __syncthreads();
+        const uint32_t c = aux->chunk, epoch = aux->epoch;
+        if (!block_acquire<ROWS, N, THREADS>(p, buf, aux, c, epoch)) return;
+        const bool ok = filter_block(p, buf, aux, ex, c, epoch, warp, lane);
+        __syncthreads();
+        if (ok) block_store<ROWS, N, THREADS>(p, buf, c);
+    }
+
+    // exchange helpers: publish this thread's per-parity values, barrier, read the previous row's
+    __device__ __forceinline__ static void exchange(Smem* ex, int slot, int r, int p0, const float (&mine)[NPAR],
+                                                    float (&prev)[NPAR]) {
+#pragma unroll
+        for (int h = 0; h < NPAR; ++h) ex->xch.v[slot][r][p0 + h] = mine[h];
+        named_barrier_rows(NW);
+#pragma unroll
+        for (int h = 0; h < NPAR; ++h) prev[h] = (r > 0) ? ex->xch.v[slot][r - 1][p0 + h] : 0.f;
+    }
+
+    __device__ static bool filter_block(const IirParams& p, float* buf, BlockAux* aux, Smem* ex, uint32_t c,
+                                        uint32_t epoch, int warp, int lane) {
+        const bool row_warp = warp > 0;
+        const int w = warp - 1;
+        const int rl = SPLIT ? (lane >> 1) : lane;       // row within the warp
+        const int r = w * RW + rl;                         // row within the chunk
+        const int p0 = SPLIT ? (lane & 1) : 0;             // first parity handled
+        float u[NPAR][M];
+        float Xp0 = 0.f, Xp1 = 0.f;  // previous section's incoming state (row-0 input history)
+        int slot = 0;
+        for (int sec = 0; sec < p.n_sections; ++sec) {
+            const IirSection& q = p.sec[sec];
+            const float4* tab = p.tables + sec * IIR_TAB_STRIDE;
+            const float4 Gw = tab[IIR_TAB_GPOW + RW - 1];
+            float s0[NPAR], s1[NPAR];
+            if (row_warp) {
+                // ---- FIR + first double-sided round -> u (own parity halves) ----
+                const float g = (sec == 0) ? p.gain : 1.f;
+                float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
+                if (r > 0) {
+                    x4 = buf[swz<N>(r - 1, N - 4)] * g;
+                    x3 = buf[swz<N>(r - 1, N - 3)] * g;
+                    x2 = buf[swz<N>(r - 1, N - 2)] * g;
+                    x1 = buf[swz<N>(r - 1, N - 1)] * g;
+                } else if (sec == 0) {
+                    x4 = x3 = 0.f;
+                    if (c > 0) {
+                        const long long cs = static_cast<long long>(c) * (ROWS * N);
+                        x2 = __ldg(p.x + cs - 2) * g;
+                        x1 = __ldg(p.x + cs - 1) * g;
+                    } else {
+                        x2 = x1 = 0.f;
+                    }
+                } else {
+                    x4 = x3 = 0.f;
+                    x2 = Xp0;
+                    x1 = Xp1;
+                }
+                const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
+                // w[-2], w[-1]: zero before the chunk (zero-padded system), else the FIR
+                float w2 = (r > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
+                float w1 = (r > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+#pragma unroll
+                for (int j = 0; j < N / 4; ++j) {
+                    const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+                    const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int n = 4 * j + k;
+                        const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
+                        const int par = n & 1;
+                        if (SPLIT) {
+                            if (par == p0) u[0][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                        } else {
+                            u[par][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                        }
+                        x2 = x1;
+                        x1 = xs[k];
+                        w2 = w1;
+                        w1 = wn;
+                    }
+                }
+                // ---- elimination levels 1 .. L-1 (one cross-row exchange per level) ----
+#pragma unroll(UNROLL ? 8 : 1)
+                for (int k = 1; k < L; ++k) {
+                    const int h = 1 << (k - 1);
+                    float mine[NPAR], prev[NPAR];
+#pragma unroll
+                    for (int hh = 0; hh < NPAR; ++hh) mine[hh] = u[hh][M - 1];
+                    exchange(ex, slot, r, p0, mine, prev);
+                    slot ^= 1;
+#pragma unroll
+                    for (int hh = 0; hh < NPAR; ++hh) Half::eliminate(u[hh], h, q.cr_r[k], q.cr_e[k], prev[hh]);
+                }
+                // ---- top level: Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t across rows ----
+#pragma unroll
+                for (int hh = 0; hh < NPAR; ++hh) {
+                    s0[hh] = 0.f;
+                    s1[hh] = u[hh][M - 1];
+                    warp_scan2<RW, TPR>(s0[hh], s1[hh], q.M, rl);
+                }
+                if (SPLIT) {
+                    if (rl == RW - 1) {
+                        aux->wtot[w][p0][0] = s0[0];
+                        aux->wtot[w][p0][1] = s1[0];
+                    }
+                } else if (lane == 31) {
+                    aux->wtot[w][0][0] = s0[0];
+                    aux->wtot[w][0][1] = s1[0];
+                    aux->wtot[w][1][0] = s0[NPAR - 1];
+                    aux->wtot[w][1][1] = s1[NPAR - 1];
+                }
+            }
+            __syncthreads();  // (A)
+            if (row_warp) {
+#pragma unroll
+                for (int hh = 0; hh < NPAR; ++hh) {
+                    float i0, i1;
+                    warp_incoming(aux, w, p0 + hh, Gw, i0, i1);
+                    if (w > 0) {
+                        float e0, e1;
+                        mv2(tab[IIR_TAB_GPOW + rl], i0, i1, e0, e1);
+                        s0[hh] += e0;
+                        s1[hh] += e1;
+                    }
+                }
+            } else {
+                control_section<NW, 2>(p, aux, sec, c, epoch, tab, Gw);
+            }
+            __syncthreads();  // (B)
+            if (aux->bail) return false;
+            const float X0 = aux->X[0], X1 = aux->X[1];
+            if (row_warp) {
+                // ---- back-substitution L-1 .. 1 (zero-padded chunk) ----
+#pragma unroll
+                for (int hh = 0; hh < NPAR; ++hh) u[hh][M - 1] = s1[hh];
+#pragma unroll(UNROLL ? 8 : 1)
+                for (int k = L - 1; k >= 1; --k) {
+                    const int h = 1 << (k - 1);
+                    // value the next row needs: y at half position M-1-2h (two rows back at the top)
+                    float mine[NPAR], prev[NPAR];
+#pragma unroll
+                    for (int hh = 0; hh < NPAR; ++hh) mine[hh] = (2 * h == M) ? s0[hh] : u[hh][M - 1 - 2 * h];
+                    exchange(ex, slot, r, p0, mine, prev);
+                    slot ^= 1;
+#pragma unroll
+                    for (int hh = 0; hh < NPAR; ++hh) Half::backsub(u[hh], h, q.cr_c[k], q.cr_d[k], s0[hh], prev[hh]);
+                }
+                // ---- response to the chunk's incoming state X (recurrence of the section) ----
+                float d2 = X0, d1 = X1;  // (delta[-2], delta[-1]) at the row start
+                if (r > 0) mv2(tab[IIR_TAB_CPOW + r - 1], X0, X1, d2, d1);
+                const float a1 = q.a1, a2 = q.a2;
+                if (SPLIT) {
+                    // stride-2 recurrence of this parity: delta[2m+p] from (delta[p], delta[p+2])
+                    const float e0s = fmaf(a1, d1, a2 * d2);   // delta[0]
+                    const float e1s = fmaf(a1, e0s, a2 * d1);  // delta[1]
+                    const float e2s = fmaf(a1, e1s, a2 * e0s); // delta[2]
+                    const float e3s = fmaf(a1, e2s, a2 * e1s); // delta[3]
+                    float dm2 = p0 ? e1s : e0s, dm1 = p0 ? e3s : e2s;
+                    const float al1 = q.ha1, al2 = q.ha2;  // -e_1, -f_1
+                    u[0][0] += dm2;
+                    u[0][1] += dm1;
+#pragma unroll(UNROLL ? 64 : 1)
+                    for (int m = 2; m < M; ++m) {
+                        const float dn = fmaf(al1, dm1, al2 * dm2);
+                        dm2 = dm1;
+                        dm1 = dn;
+                        u[0][m] += dn;
+                    }
+                    // write this parity's samples of the row
+#pragma unroll(UNROLL ? 64 : 1)
+                    for (int m = 0; m < M; ++m) buf[swz<N>(r, 2 * m + p0)] = u[0][m];
+                } else {
+#pragma unroll
+                    for (int n = 0; n < N; ++n) {
+                        const float dn = fmaf(a1, d1, a2 * d2);
+                        d2 = d1;
+                        d1 = dn;
+                        u[n & 1][n >> 1] += dn;
+                    }
+#pragma unroll
+                    for (int j = 0; j < N / 4; ++j)
+                        *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j)) =
+                            make_float4(u[0][2 * j], u[1][2 * j], u[0][2 * j + 1], u[1][2 * j + 1]);
+                }
+                Xp0 = X0;
+                Xp1 = X1;
+                named_barrier_rows(NW);  // rows written before the next section reads histories
+            }
+        }
+        if (row_warp) fence_proxy_async_smem();
+        return true;
+    }
+};
+
+}  // namespace iirgb

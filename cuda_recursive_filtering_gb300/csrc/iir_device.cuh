@@ -424,6 +424,16 @@ struct BlockGeom {
     }
 };
 
+// Resident blocks per SM that shared memory (227 KB), threads (2048) and the occupancy
+// target allow: the __launch_bounds__ minimum for a kernel of `threads` threads.
+constexpr int min_blocks_for(size_t smem_bytes, int threads) {
+    const int by_smem = static_cast<int>((227 * 1024) / smem_bytes);
+    const int by_thr = 2048 / threads;
+    int b = by_smem < by_thr ? by_smem : by_thr;
+    if (b > IIR_MAX_BLOCKS_PER_SM) b = IIR_MAX_BLOCKS_PER_SM;
+    return b < 1 ? 1 : b;
+}
+
 // Float index of sample n of row r in the swizzled chunk buffer (128B swizzle: the 16-byte
 // unit u of line L lives at unit u ^ (L & 7)).
 template <int N>

@@ -1,5 +1,40 @@
-#include "iir_device.cuh"
+// iir_dtcr.cu — DTCR realization for sm_103a (cyclic-reduction row solver in iir_cr.cuh).
+//
+// Reference: include/dtcr_kernels.cuh. DTCR: the first elimination round is fused into the FIR pass and the even / odd halves run concurrently on the two threads of a row (dtcr_kernels.cuh:291-657, 2500-2904); loop form DTCR_*_LOOP, register form DTCR_*_UNROLL_* (dtcr_kernels.cuh:660-3521).
+#include "iir_cr.cuh"
 #include "iir_registry.h"
+
 namespace iirgb {
-void register_dtcr(std::vector<KernelEntry>&) {}
+
+template <int N, int ROWS, bool UNROLL>
+__global__ void __launch_bounds__(CrBlock<true, 32, N, ROWS, UNROLL>::THREADS,
+                                  min_blocks_for(CrBlock<true, 32, N, ROWS, UNROLL>::SMEM_BYTES,
+                                                 CrBlock<true, 32, N, ROWS, UNROLL>::THREADS))
+    iir_dtcr_kernel(const __grid_constant__ IirParams p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    CrBlock<true, 32, N, ROWS, UNROLL>::run(p, smem);
 }
+
+// A tile of BLOCK_SIZE rows is the reference's chunk; a block filters ROWS rows (several
+// tiles), so BLOCK_SIZE = 32 and 64 share one instantiation per N.
+template <int N, int ROWS, bool UNROLL>
+static void add(std::vector<KernelEntry>& reg) {
+    using Blk = CrBlock<true, 32, N, ROWS, UNROLL>;
+    const int kind = UNROLL ? IIR_KIND_DTCR_UNROLL : IIR_KIND_DTCR;
+    for (int b : {32, 64})
+        reg.push_back(KernelEntry{kind, b, N, (const void*)iir_dtcr_kernel<N, ROWS, UNROLL>, Blk::THREADS, Blk::SMEM_BYTES,
+                                  0, ROWS});
+}
+
+void register_dtcr(std::vector<KernelEntry>& reg) {
+    add<16, 128, false>(reg);
+    add<32, 128, false>(reg);
+    add<64, 128, false>(reg);
+    add<128, 64, false>(reg);
+    add<16, 128, true>(reg);
+    add<32, 128, true>(reg);
+    add<64, 128, true>(reg);
+    add<128, 64, true>(reg);
+}
+
+}  // namespace iirgb

@@ -164,6 +164,10 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
             const double en = 2.0 * f - e * e, fn = f * f;
             e = en;
             f = fn;
+            if (k == 1) {
+                q.ha1 = static_cast<float>(-e);
+                q.ha2 = static_cast<float>(-f);
+            }
             if (k < L) {
                 if (!(std::fabs(e) > 1e-30)) return IIR_ERR_UNSUPPORTED;  // singular elimination
                 q.cr_r[k] = static_cast<float>(f / e);

@@ -50,7 +50,7 @@ struct IirSection {
     float e0, f0;           // e_0 = -a1, f_0 = -a2 (first double-sided round)
     float fir5[4];          // fused FIR + first CR round taps D1..D4 (DTCR)
     float top_e, top_f;     // top-level recurrence across rows: Y_t + e_L Y_{t-1} + f_L Y_{t-2}
-    float pad[2];
+    float ha1, ha2;         // parity-half recurrence after the first round: -e_1, -f_1
 };
 
 struct IirParams {

@@ -148,3 +148,25 @@ def test_config1_order2(cuda_device):
     for kernel in ("PH", "DTCR"):
         e = oracle.errors(sosfilt(sos, xt, kernel=kernel).cpu().numpy(), ref)
         assert e["rel_rms"] <= 1e-5, (kernel, e)
+
+
+@pytest.mark.parametrize("family", ["STCR", "DTCR"])
+@pytest.mark.parametrize("geom", GEOMS, ids=lambda g: f"{g[0]}x{g[1]}")
+@pytest.mark.parametrize("order", ORDERS)
+def test_loop_and_unrolled_forms_bit_identical(family, geom, order, cuda_device):
+    """Loop and register (hand-unrolled) forms execute the same operations in the same order:
+    identical bits, as the reference's emulator shows for its STCR forms
+    (tools/stcr_emulator.py:343-347). Bit identity holds per launch; the decoupled lookback
+    may compose a chunk's carry from different predecessors in different launches, so both
+    forms run on a single-chunk input here and on a multi-chunk input with a tolerance."""
+    sos = butter(order)
+    rows = 64 if geom[1] == 128 else 128
+    for n, exact in ((rows * geom[1], True), (7 * rows * geom[1] + 5, False)):
+        x = np.random.default_rng(order + n).uniform(-1, 1, n).astype(np.float32)
+        a = run_plan(Plan(sos, family, *geom, max_n=n), x)
+        b = run_plan(Plan(sos, family + "_UNROLL", *geom, max_n=n), x)
+        if exact:
+            assert np.array_equal(a, b)
+        else:
+            ref = golden(sos, x)
+            assert np.max(np.abs(a.astype(np.float64) - b)) <= 1e-6 * np.max(np.abs(ref))
