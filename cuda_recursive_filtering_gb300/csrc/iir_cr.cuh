@@ -31,12 +31,6 @@
 
 namespace iirgb {
 
-// Exchange area for cross-row values, double buffered per level: [2][ROWS][2 parities].
-template <int ROWS>
-struct CrExchange {
-    float v[2][ROWS][2];
-};
-
 // One parity half of a row. u[] holds the half's values (half index m).
 template <int M, bool UNROLL>
 struct CrHalf {
@@ -80,65 +74,65 @@ constexpr int ilog2_c(int v) { return v <= 1 ? 0 : 1 + ilog2_c(v / 2); }
 // STCR (SPLIT = false): one thread per row holds both parity halves.
 // DTCR (SPLIT = true): the two halves of a row run on two neighbouring lanes (dim3(B, 2) in
 // the reference, dtcr_kernels.cuh:56), interleaved so a row's pair shares a warp.
+//
+// Each row warp solves its rows as a zero-padded tile (zero state before the tile): the
+// cross-row values of the elimination, the top-level scan and the back-substitution move by
+// warp shuffles only. Tiles are then joined like chunks: tile w's true incoming state is
+// S_w = C^(RW w) X + sum_{v<w} C^(RW (w-1-v)) P_v (P_v = tile v's zero-state end pair,
+// X = the chunk's incoming state from the lookback), and every row adds the response of the
+// section recurrence to its own incoming pair C^(row) S_w.
 template <bool SPLIT, int B_, int N_, int ROWS_, bool UNROLL>
 struct CrBlock {
     static constexpr int B = B_, N = N_, ROWS = ROWS_, M = N_ / 2, L = ilog2_c(N_);
     static constexpr int TPR = SPLIT ? 2 : 1;   // threads per row
     static constexpr int NPAR = SPLIT ? 1 : 2;  // parity halves per thread
-    static constexpr int RW = 32 / TPR;         // rows per warp
+    static constexpr int RW = 32 / TPR;         // rows per warp (tile)
     static constexpr int NW = ROWS * TPR / 32;  // row warps
     static constexpr int THREADS = 32 + NW * 32;
     static_assert(ROWS % RW == 0 && NW <= 16 && ROWS <= IIR_MAX_ROWS, "rows per chunk");
     using Half = CrHalf<M, UNROLL>;
-
-    struct Smem {
-        CrExchange<ROWS> xch;
-    };
-    static constexpr size_t SMEM_BYTES = BlockGeom<ROWS, N>::SMEM_BYTES + sizeof(Smem);
-
-    __device__ static Smem* extra(unsigned char* smem) {
-        return reinterpret_cast<Smem*>(block_aux<ROWS, N>(smem) + 1);
-    }
+    static constexpr size_t SMEM_BYTES = BlockGeom<ROWS, N>::SMEM_BYTES;
+    // occupancy target: the register form keeps NPAR * M values per thread in registers
+    static constexpr int REGS_WANTED = (UNROLL ? NPAR * M : 0) + 48;
+    static constexpr int MIN_BLOCKS_REGS = 65536 / (THREADS * (REGS_WANTED < 64 ? 64 : REGS_WANTED));
+    static constexpr int MIN_BLOCKS = min_blocks_for(SMEM_BYTES, THREADS) < MIN_BLOCKS_REGS
+                                          ? min_blocks_for(SMEM_BYTES, THREADS)
+                                          : (MIN_BLOCKS_REGS < 1 ? 1 : MIN_BLOCKS_REGS);
 
     __device__ static void run(const IirParams& p, unsigned char* smem) {
         float* buf = chunk_buffer<ROWS, N>(smem);
         BlockAux* aux = block_aux<ROWS, N>(smem);
-        Smem* ex = extra(smem);
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
         if (warp == 0) block_begin<ROWS, N>(p, buf, aux);
         __syncthreads();
         const uint32_t c = aux->chunk, epoch = aux->epoch;
         if (!block_acquire<ROWS, N, THREADS>(p, buf, aux, c, epoch)) return;
-        const bool ok = filter_block(p, buf, aux, ex, c, epoch, warp, lane);
+        const bool ok = filter_block(p, buf, aux, c, epoch, warp, lane);
         __syncthreads();
         if (ok) block_store<ROWS, N, THREADS>(p, buf, c);
     }
 
-    // exchange helpers: publish this thread's per-parity values, barrier, read the previous row's
-    __device__ __forceinline__ static void exchange(Smem* ex, int slot, int r, int p0, const float (&mine)[NPAR],
-                                                    float (&prev)[NPAR]) {
-#pragma unroll
-        for (int h = 0; h < NPAR; ++h) ex->xch.v[slot][r][p0 + h] = mine[h];
-        named_barrier_rows(NW);
-#pragma unroll
-        for (int h = 0; h < NPAR; ++h) prev[h] = (r > 0) ? ex->xch.v[slot][r - 1][p0 + h] : 0.f;
+    // previous row (same parity) of the tile, zero before the tile's first row
+    __device__ __forceinline__ static float prev_row(float v, int rl) {
+        const float o = __shfl_up_sync(FULL_MASK, v, TPR);
+        return rl > 0 ? o : 0.f;
     }
 
-    __device__ static bool filter_block(const IirParams& p, float* buf, BlockAux* aux, Smem* ex, uint32_t c,
-                                        uint32_t epoch, int warp, int lane) {
+    __device__ static bool filter_block(const IirParams& p, float* buf, BlockAux* aux, uint32_t c, uint32_t epoch,
+                                        int warp, int lane) {
         const bool row_warp = warp > 0;
         const int w = warp - 1;
-        const int rl = SPLIT ? (lane >> 1) : lane;       // row within the warp
-        const int r = w * RW + rl;                         // row within the chunk
-        const int p0 = SPLIT ? (lane & 1) : 0;             // first parity handled
+        const int rl = SPLIT ? (lane >> 1) : lane;  // row within the tile (warp)
+        const int r = w * RW + rl;                    // row within the chunk
+        const int p0 = SPLIT ? (lane & 1) : 0;        // first parity handled
         float u[NPAR][M];
         float Xp0 = 0.f, Xp1 = 0.f;  // previous section's incoming state (row-0 input history)
-        int slot = 0;
         for (int sec = 0; sec < p.n_sections; ++sec) {
             const IirSection& q = p.sec[sec];
             const float4* tab = p.tables + sec * IIR_TAB_STRIDE;
-            const float4 Gw = tab[IIR_TAB_GPOW + RW - 1];
+            const float4 Ct = tab[IIR_TAB_CPOW + RW - 1];  // tile transition C^RW
             float s0[NPAR], s1[NPAR];
+            float P0 = 0.f, P1 = 0.f;  // tile zero-state end pair (valid in the tile's last row)
             if (row_warp) {
                 // ---- FIR + first double-sided round -> u (own parity halves) ----
                 const float g = (sec == 0) ? p.gain : 1.f;
@@ -163,9 +157,9 @@ struct CrBlock {
                     x1 = Xp1;
                 }
                 const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
-                // w[-2], w[-1]: zero before the chunk (zero-padded system), else the FIR
-                float w2 = (r > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
-                float w1 = (r > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+                // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
+                float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
+                float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
 #pragma unroll
                 for (int j = 0; j < N / 4; ++j) {
                     const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
@@ -186,82 +180,78 @@ struct CrBlock {
                         w1 = wn;
                     }
                 }
-                // ---- elimination levels 1 .. L-1 (one cross-row exchange per level) ----
+                // ---- elimination levels 1 .. L-1 (previous row's kept tail by shuffle) ----
 #pragma unroll(UNROLL ? 8 : 1)
                 for (int k = 1; k < L; ++k) {
                     const int h = 1 << (k - 1);
-                    float mine[NPAR], prev[NPAR];
 #pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) mine[hh] = u[hh][M - 1];
-                    exchange(ex, slot, r, p0, mine, prev);
-                    slot ^= 1;
-#pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) Half::eliminate(u[hh], h, q.cr_r[k], q.cr_e[k], prev[hh]);
+                    for (int hh = 0; hh < NPAR; ++hh) {
+                        const float prev = prev_row(u[hh][M - 1], rl);
+                        Half::eliminate(u[hh], h, q.cr_r[k], q.cr_e[k], prev);
+                    }
                 }
-                // ---- top level: Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t across rows ----
+                // ---- top level across the tile's rows: Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t ----
 #pragma unroll
                 for (int hh = 0; hh < NPAR; ++hh) {
                     s0[hh] = 0.f;
                     s1[hh] = u[hh][M - 1];
                     warp_scan2<RW, TPR>(s0[hh], s1[hh], q.M, rl);
+                    u[hh][M - 1] = s1[hh];
                 }
-                if (SPLIT) {
-                    if (rl == RW - 1) {
-                        aux->wtot[w][p0][0] = s0[0];
-                        aux->wtot[w][p0][1] = s1[0];
+                // ---- back-substitution L-1 .. 1 (zero-padded tile) ----
+#pragma unroll(UNROLL ? 8 : 1)
+                for (int k = L - 1; k >= 1; --k) {
+                    const int h = 1 << (k - 1);
+#pragma unroll
+                    for (int hh = 0; hh < NPAR; ++hh) {
+                        // y at half position -1 - 2h: previous row's, or two rows back at the top
+                        const float far = prev_row((2 * h == M) ? s0[hh] : u[hh][M - 1 - 2 * h], rl);
+                        Half::backsub(u[hh], h, q.cr_c[k], q.cr_d[k], s0[hh], far);
                     }
-                } else if (lane == 31) {
-                    aux->wtot[w][0][0] = s0[0];
-                    aux->wtot[w][0][1] = s1[0];
-                    aux->wtot[w][1][0] = s0[NPAR - 1];
-                    aux->wtot[w][1][1] = s1[NPAR - 1];
+                }
+                // tile end pair (y[N-2], y[N-1]) of the last row
+                if (SPLIT) {
+                    const float mine = u[0][M - 1];
+                    const float other = __shfl_xor_sync(FULL_MASK, mine, 1);
+                    P0 = p0 ? other : mine;
+                    P1 = p0 ? mine : other;
+                } else {
+                    P0 = u[0][M - 1];
+                    P1 = u[1][M - 1];
+                }
+                if (lane == 31) {
+                    aux->wtot[w][0][0] = P0;
+                    aux->wtot[w][0][1] = P1;
                 }
             }
             __syncthreads();  // (A)
+            float in0 = 0.f, in1 = 0.f;  // zero-state incoming pair of this tile
             if (row_warp) {
-#pragma unroll
-                for (int hh = 0; hh < NPAR; ++hh) {
-                    float i0, i1;
-                    warp_incoming(aux, w, p0 + hh, Gw, i0, i1);
-                    if (w > 0) {
-                        float e0, e1;
-                        mv2(tab[IIR_TAB_GPOW + rl], i0, i1, e0, e1);
-                        s0[hh] += e0;
-                        s1[hh] += e1;
-                    }
-                }
+                warp_incoming(aux, w, 0, Ct, in0, in1);
             } else {
-                control_section<NW, 2>(p, aux, sec, c, epoch, tab, Gw);
+                control_section<NW, 1>(p, aux, sec, c, epoch, tab, Ct);
             }
             __syncthreads();  // (B)
             if (aux->bail) return false;
             const float X0 = aux->X[0], X1 = aux->X[1];
             if (row_warp) {
-                // ---- back-substitution L-1 .. 1 (zero-padded chunk) ----
-#pragma unroll
-                for (int hh = 0; hh < NPAR; ++hh) u[hh][M - 1] = s1[hh];
-#pragma unroll(UNROLL ? 8 : 1)
-                for (int k = L - 1; k >= 1; --k) {
-                    const int h = 1 << (k - 1);
-                    // value the next row needs: y at half position M-1-2h (two rows back at the top)
-                    float mine[NPAR], prev[NPAR];
-#pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) mine[hh] = (2 * h == M) ? s0[hh] : u[hh][M - 1 - 2 * h];
-                    exchange(ex, slot, r, p0, mine, prev);
-                    slot ^= 1;
-#pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) Half::backsub(u[hh], h, q.cr_c[k], q.cr_d[k], s0[hh], prev[hh]);
+                // true incoming pair of the tile, then of this row
+                float S0 = X0, S1 = X1;
+                if (w > 0) {
+                    float t0, t1;
+                    mv2(tab[IIR_TAB_CPOW + RW * w - 1], X0, X1, t0, t1);
+                    S0 = t0 + in0;
+                    S1 = t1 + in1;
                 }
-                // ---- response to the chunk's incoming state X (recurrence of the section) ----
-                float d2 = X0, d1 = X1;  // (delta[-2], delta[-1]) at the row start
-                if (r > 0) mv2(tab[IIR_TAB_CPOW + r - 1], X0, X1, d2, d1);
+                float d2 = S0, d1 = S1;  // (delta[-2], delta[-1]) at the row start
+                if (rl > 0) mv2(tab[IIR_TAB_CPOW + rl - 1], S0, S1, d2, d1);
                 const float a1 = q.a1, a2 = q.a2;
                 if (SPLIT) {
                     // stride-2 recurrence of this parity: delta[2m+p] from (delta[p], delta[p+2])
-                    const float e0s = fmaf(a1, d1, a2 * d2);   // delta[0]
-                    const float e1s = fmaf(a1, e0s, a2 * d1);  // delta[1]
-                    const float e2s = fmaf(a1, e1s, a2 * e0s); // delta[2]
-                    const float e3s = fmaf(a1, e2s, a2 * e1s); // delta[3]
+                    const float e0s = fmaf(a1, d1, a2 * d2);    // delta[0]
+                    const float e1s = fmaf(a1, e0s, a2 * d1);   // delta[1]
+                    const float e2s = fmaf(a1, e1s, a2 * e0s);  // delta[2]
+                    const float e3s = fmaf(a1, e2s, a2 * e1s);  // delta[3]
                     float dm2 = p0 ? e1s : e0s, dm1 = p0 ? e3s : e2s;
                     const float al1 = q.ha1, al2 = q.ha2;  // -e_1, -f_1
                     u[0][0] += dm2;
@@ -273,9 +263,18 @@ struct CrBlock {
                         dm1 = dn;
                         u[0][m] += dn;
                     }
-                    // write this parity's samples of the row
+                    // write the row as float2 pairs (2m, 2m+1): even m by parity 0, odd m by parity 1
 #pragma unroll(UNROLL ? 64 : 1)
-                    for (int m = 0; m < M; ++m) buf[swz<N>(r, 2 * m + p0)] = u[0][m];
+                    for (int m = 0; m < M; m += 2) {
+                        const float a = u[0][m], b = u[0][m + 1];
+                        const float oa = __shfl_xor_sync(FULL_MASK, a, 1);
+                        const float ob = __shfl_xor_sync(FULL_MASK, b, 1);
+                        // parity 0 holds even samples: pair for m is (a, oa); parity 1's for m+1 is (ob, b)
+                        if (p0 == 0)
+                            *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m)) = make_float2(a, oa);
+                        else
+                            *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m + 2)) = make_float2(ob, b);
+                    }
                 } else {
 #pragma unroll
                     for (int n = 0; n < N; ++n) {

@@ -8,8 +8,7 @@ namespace iirgb {
 
 template <int N, int ROWS, bool UNROLL>
 __global__ void __launch_bounds__(CrBlock<true, 32, N, ROWS, UNROLL>::THREADS,
-                                  min_blocks_for(CrBlock<true, 32, N, ROWS, UNROLL>::SMEM_BYTES,
-                                                 CrBlock<true, 32, N, ROWS, UNROLL>::THREADS))
+                                  CrBlock<true, 32, N, ROWS, UNROLL>::MIN_BLOCKS)
     iir_dtcr_kernel(const __grid_constant__ IirParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
     CrBlock<true, 32, N, ROWS, UNROLL>::run(p, smem);
@@ -27,14 +26,14 @@ static void add(std::vector<KernelEntry>& reg) {
 }
 
 void register_dtcr(std::vector<KernelEntry>& reg) {
-    add<16, 128, false>(reg);
-    add<32, 128, false>(reg);
-    add<64, 128, false>(reg);
-    add<128, 64, false>(reg);
-    add<16, 128, true>(reg);
-    add<32, 128, true>(reg);
-    add<64, 128, true>(reg);
-    add<128, 64, true>(reg);
+    add<16, 64, false>(reg);
+    add<32, 64, false>(reg);
+    add<64, 64, false>(reg);
+    add<128, 32, false>(reg);
+    add<16, 64, true>(reg);
+    add<32, 64, true>(reg);
+    add<64, 64, true>(reg);
+    add<128, 32, true>(reg);
 }
 
 }  // namespace iirgb

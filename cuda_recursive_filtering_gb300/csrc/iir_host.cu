@@ -279,7 +279,7 @@ int default_geometry(int kind, int n_sections, int& B, int& N) {
     if (kind == IIR_KIND_PLR) {
         const int order = 2 * n_sections;
         if (B <= 0) B = order <= 2 ? 512 : order <= 4 ? 256 : order <= 8 ? 128 : 64;
-        if (N <= 0) N = 8;
+        if (N <= 0) N = 8;  // values per thread (PLR_X)
         return IIR_OK;
     }
     if (B <= 0) B = 32;
@@ -300,8 +300,8 @@ size_t chunk_samples(const iir_plan* p) {
 
 // 64-bit words of carry slots per section (chunk slots, then one slot per group of chunks)
 size_t carry_words_per_section(const iir_plan* p, size_t cap_chunks) {
-    if (p->kind == IIR_KIND_PLR) return 2 * static_cast<size_t>(p->order) * cap_chunks;
-    return 4 * (cap_chunks + cap_chunks / IIR_GROUP + 2);
+    const size_t w = (p->kind == IIR_KIND_PLR) ? 2 * static_cast<size_t>(p->order) : 4;
+    return w * (cap_chunks + cap_chunks / IIR_GROUP + 2);
 }
 
 int alloc_carry(iir_plan* p, size_t cap_chunks, cudaStream_t stream) {
@@ -349,10 +349,9 @@ void plan_free(iir_plan* p) {
     delete p;
 }
 
-// PLR: n-nacci factor arrays fac_j[i], the response at offset i of the order-k recurrence
-// to a unit initial condition y[-k+j] = 1 (plr_kernels.cuh:149-409, there in float32).
-void plr_factors(const double* a, int order, int chunk, std::vector<float>& fac) {
-    fac.assign(static_cast<size_t>(order) * chunk, 0.f);
+// FP64 factor arrays (all chunk offsets) and chunk transition Phi[i][j] = fac_j[chunk-k+i].
+void plr_factors_f64(const double* a, int order, int chunk, std::vector<double>& fac) {
+    fac.assign(static_cast<size_t>(order) * chunk, 0.0);
     std::vector<double> v(static_cast<size_t>(chunk) + order);
     for (int j = 0; j < order; ++j) {
         std::fill(v.begin(), v.end(), 0.0);
@@ -362,8 +361,18 @@ void plr_factors(const double* a, int order, int chunk, std::vector<float>& fac)
             for (int m = 0; m < order; ++m) acc += a[m] * v[i - 1 - m];
             v[i] = acc;
         }
-        for (int i = 0; i < chunk; ++i) fac[static_cast<size_t>(j) * chunk + i] = static_cast<float>(v[i + order]);
+        for (int i = 0; i < chunk; ++i) fac[static_cast<size_t>(j) * chunk + i] = v[i + order];
     }
+}
+
+void matmul_k(const std::vector<double>& A, const std::vector<double>& B, std::vector<double>& C, int k) {
+    std::vector<double> R(static_cast<size_t>(k) * k, 0.0);
+    for (int i = 0; i < k; ++i)
+        for (int m = 0; m < k; ++m) {
+            const double aim = A[static_cast<size_t>(i) * k + m];
+            for (int j = 0; j < k; ++j) R[static_cast<size_t>(i) * k + j] += aim * B[static_cast<size_t>(m) * k + j];
+        }
+    C.swap(R);
 }
 
 int plan_create_plr(iir_plan** out, const double* b, const double* a, int order, double gain, int B, int X,
@@ -386,10 +395,37 @@ int plan_create_plr(iir_plan** out, const double* b, const double* a, int order,
         return st;
     }
     const int chunk = Bd * Xd;
-    std::vector<float> fac;
-    plr_factors(a, order, chunk, fac);
-    st = cuda_status(cudaMalloc(&p->d_fac, fac.size() * sizeof(float)));
-    if (!st) st = cuda_status(cudaMemcpy(p->d_fac, fac.data(), fac.size() * sizeof(float), cudaMemcpyHostToDevice));
+    const int k = order;
+    std::vector<double> fac;
+    plr_factors_f64(a, order, chunk, fac);
+    // Phi and its powers (FP64), rounded once
+    std::vector<double> phi(static_cast<size_t>(k) * k), P(static_cast<size_t>(k) * k, 0.0), Pg, phig;
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j)
+            phi[static_cast<size_t>(i) * k + j] = fac[static_cast<size_t>(j) * chunk + (chunk - k + i)];
+    std::vector<float> tables(2 * 33 * static_cast<size_t>(k) * k);
+    for (int i = 0; i < k; ++i) P[static_cast<size_t>(i) * k + i] = 1.0;
+    for (int l = 0; l <= 32; ++l) {
+        for (size_t q = 0; q < P.size(); ++q) tables[static_cast<size_t>(l) * k * k + q] = static_cast<float>(P[q]);
+        matmul_k(P, phi, P, k);
+    }
+    phig = phi;  // Phi^32
+    for (int sq = 0; sq < 5; ++sq) matmul_k(phig, phig, phig, k);
+    Pg.assign(static_cast<size_t>(k) * k, 0.0);
+    for (int i = 0; i < k; ++i) Pg[static_cast<size_t>(i) * k + i] = 1.0;
+    for (int l = 0; l <= 32; ++l) {
+        for (size_t q = 0; q < Pg.size(); ++q)
+            tables[(33 + static_cast<size_t>(l)) * k * k + q] = static_cast<float>(Pg[q]);
+        matmul_k(Pg, phig, Pg, k);
+    }
+    std::vector<float> facf(fac.size());
+    for (size_t i = 0; i < fac.size(); ++i) facf[i] = static_cast<float>(fac[i]);
+    const size_t fac_bytes = facf.size() * sizeof(float), tab_bytes = tables.size() * sizeof(float);
+    st = cuda_status(cudaMalloc(&p->d_fac, fac_bytes + tab_bytes));
+    if (!st) st = cuda_status(cudaMemcpy(p->d_fac, facf.data(), fac_bytes, cudaMemcpyHostToDevice));
+    if (!st)
+        st = cuda_status(cudaMemcpy(reinterpret_cast<char*>(p->d_fac) + fac_bytes, tables.data(), tab_bytes,
+                                    cudaMemcpyHostToDevice));
     if (st) {
         plan_free(p);
         return st;
@@ -398,6 +434,8 @@ int plan_create_plr(iir_plan** out, const double* b, const double* a, int order,
     std::memset(&q, 0, sizeof(q));
     q.state = p->d_state;
     q.fac = p->d_fac;
+    q.pc = p->d_fac + facf.size();
+    q.pg = q.pc + 33 * static_cast<size_t>(k) * k;
     q.chunk = chunk;
     q.gain = static_cast<float>(gain);
     for (int j = 0; j < order; ++j) {

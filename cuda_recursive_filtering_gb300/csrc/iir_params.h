@@ -80,9 +80,11 @@ struct IirPlrParams {
     const float* x;
     float* y;
     long long n;
-    unsigned long long* carry;        // [carry_cap][2][k] flag|value words (part, full)
+    unsigned long long* carry;        // [carry_cap][2k] chunk slots (part, full), then group slots
     IirLaunchState* state;
     const float* fac;                 // [k][chunk] n-nacci factor arrays (fac[j][i])
+    const float* pc;                  // [33][k][k] chunk-transition powers Phi^l
+    const float* pg;                  // [33][k][k] group-transition powers Phi^(32 l)
     long long timeout_ns;
     long long withhold_chunk;
     unsigned int nchunks;

@@ -8,8 +8,7 @@ namespace iirgb {
 
 template <int N, int ROWS, bool UNROLL>
 __global__ void __launch_bounds__(CrBlock<false, 32, N, ROWS, UNROLL>::THREADS,
-                                  min_blocks_for(CrBlock<false, 32, N, ROWS, UNROLL>::SMEM_BYTES,
-                                                 CrBlock<false, 32, N, ROWS, UNROLL>::THREADS))
+                                  CrBlock<false, 32, N, ROWS, UNROLL>::MIN_BLOCKS)
     iir_stcr_kernel(const __grid_constant__ IirParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
     CrBlock<false, 32, N, ROWS, UNROLL>::run(p, smem);

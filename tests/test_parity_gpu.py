@@ -170,3 +170,79 @@ def test_loop_and_unrolled_forms_bit_identical(family, geom, order, cuda_device)
         else:
             ref = golden(sos, x)
             assert np.max(np.abs(a.astype(np.float64) - b)) <= 1e-6 * np.max(np.abs(ref))
+
+
+# ---------------------------------------------------------------------------------------
+# PLR (direct form, order 2K) — tools/plr_emulator.py: orders 2/4 pass the 1e-4 gate in
+# float32, order 8 is marginal (fails by a hair in the reference's sequential emulation),
+# order 16 is numerically unusable (non-finite). The verdict is reported, not forced.
+# ---------------------------------------------------------------------------------------
+@pytest.mark.parametrize("order", (2, 4))
+@pytest.mark.parametrize("X", (1, 4, 8))
+def test_plr_low_orders_pass_gate(order, X, cuda_device):
+    sos = butter(order)
+    bt = {2: 512, 4: 256}[order]
+    n = 9 * bt * X * 33 + 17
+    x = np.random.default_rng(order * 10 + X).uniform(-1, 1, n).astype(np.float32)
+    y = run_plan(Plan(sos, "PLR", bt, X, max_n=n), x)
+    e = oracle.errors(y, golden(sos, x))
+    assert e["finite"] and e["rel_max"] <= 1e-4, e
+
+
+@pytest.mark.parametrize("order", (8, 16))
+def test_plr_high_orders_report_direct_form_fragility(order, cuda_device):
+    """Runs to completion without device errors; the error is whatever float32 direct form
+    gives (the reference stores 0 GS/s for order 16 because it fails the gate)."""
+    sos = butter(order, 0.2)
+    n = 1 << 16
+    x = formats.reference_input(n, 1.0)
+    plan = Plan(sos, "PLR", max_n=n)
+    with np.errstate(all="ignore"):
+        y = run_plan(plan, x)
+        e = oracle.errors(y, golden(sos, x))
+    if order == 16:
+        assert (not e["finite"]) or e["rel_max"] > 1e-4
+    else:
+        assert (not e["finite"]) or e["rel_max"] < 1e-1
+
+
+@pytest.mark.parametrize("B", (512, 1024))
+@pytest.mark.parametrize("Xr", (1, 4, 9, 10))
+def test_plr_matches_reference_plr2_emulator(B, Xr, cuda_device):
+    """Same inputs as tools/plr_emulator.py Part A (including its ragged tail chunk)."""
+    emu = np.load(os.path.join(GOLDEN, "emulators.npz"))
+    x = emu[f"x_plr2_{B}_{Xr}"]
+    ref_emu = emu[f"plr2_{B}_{Xr}"]
+    taps = formats.parse_filter_taps(os.path.join(GOLDEN, "ref_order2", "filter_taps.hpp"))
+    from cuda_recursive_filtering_gb300 import PlrPlan
+    from scipy import signal
+    bb, aa = signal.butter(2, 0.2, output="ba")
+    plan = PlrPlan(bb[1:] / bb[0], -aa[1:], 1.0, max_n=x.size)
+    y = run_plan(plan, x)
+    g = oracle.sosfilt_f64(formats.normalise_sos(signal.butter(2, 0.2, output="sos"))[0].astype(np.float64),
+                           x.astype(np.float64))
+    scale = np.max(np.abs(g))
+    assert np.max(np.abs(y.astype(np.float64) - ref_emu)) <= 1e-5 * scale
+    assert oracle.errors(y, g)["rel_max"] <= 1e-4
+    del taps
+
+
+@pytest.mark.parametrize("order", (2, 4))
+def test_plr_from_filter_taps_hpp(order, cuda_device):
+    """PLR consumes PLR_FILTER_B / PLR_FILTER_A of the reference's filter_taps.hpp."""
+    from cuda_recursive_filtering_gb300 import PlrPlan
+    d = os.path.join(GOLDEN, f"ref_order{order}")
+    taps = formats.parse_filter_taps(os.path.join(d, "filter_taps.hpp"))
+    ref = formats.read_reference_bin(os.path.join(d, "reference.bin"))
+    x = formats.reference_input(ref.size, taps["gain"])
+    y = run_plan(PlrPlan(taps["plr_b"], taps["plr_a"], 1.0, max_n=ref.size), x)
+    assert oracle.errors(y, ref)["rel_max"] <= 1e-4
+
+
+def test_plr_repeated_launches(cuda_device):
+    sos = butter(4)
+    plan = Plan(sos, "PLR", max_n=1 << 12)
+    for i, n in enumerate([4096, 200000, 777, 1 << 18]):
+        x = np.random.default_rng(i).uniform(-1, 1, n).astype(np.float32)
+        e = oracle.errors(run_plan(plan, x), golden(sos, x))
+        assert e["rel_max"] <= 1e-4, (i, n, e)
