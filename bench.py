@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Throughput benchmark: cascaded-biquad IIR filtering on GB300.
+
+Workload (one step = one filtering pass over the whole signal): Butterworth lowpass
+(scipy butter, cutoff 0.1 x Nyquist, SOS form) over 2^28 float32 samples i.i.d.
+uniform[-1, 1) from seed 1 — the plain roofline sweep the reference benchmarks
+(GS/s, P20 of batches in src/test_performance.cu / include/measure.cuh). Headline: the DTCR
+realization at order 2 (geometry 32x64). The signal (1 GiB in + 1 GiB out) is far larger
+than L2, so no flush is needed between steps. Extra rows time every realization at orders
+2/4/8/16 on the same signal.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-sweep]
+
+Prints one JSON line (rank 0). Under torchrun every rank filters its own replica of the
+workload on its own GPU (the path has no exchange step between GPUs: replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GS/s (fp32 samples per second through the cascaded-biquad filter)"
+UNIT = "GS/s"
+LOG2N = 28
+HEADLINE = {"kernel": "DTCR_UNROLL", "order": 2, "block_size": 32, "n_blocks": 64}
+SWEEP_GEOM = {"PH": (32, 64), "STCR": (32, 64), "STCR_UNROLL": (32, 64), "DTCR": (32, 64),
+              "DTCR_UNROLL": (32, 64), "PLR": (0, 0)}
+BYTES_PER_SAMPLE = 8  # 4 read + 4 written (algorithmic)
+
+
+def peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic_per_launch() -> float | None:
+    """DRAM bytes (read + write) per launch of the headline kernel from the committed ncu
+    summary, scaled to 2^28 samples (the summary records bytes per sample)."""
+    path = os.path.join(ROOT, "profiles", "dtcr_order2_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_sample:"):
+            return float(line.split(":")[1]) * (1 << LOG2N)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_plan(plan, x, y, steps: int, warmup: int, stream):
+    import torch
+    for _ in range(warmup):
+        plan(x, y, stream=stream)
+    plan.check(stream)
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(steps):
+        plan(x, y, stream=stream)
+    e.record(stream)
+    e.synchronize()
+    torch.cuda.synchronize()
+    plan.check(stream)
+    return s.elapsed_time(e) / steps
+
+
+def cpu_baseline_sample(sos, x_cpu, budget_s: float = 10.0) -> dict:
+    """The reference's CPU golden path (FP64 cascade, tools/ref_generate.py:89 via scipy's
+    sosfilt; restated in C under oracle/) on a bounded sample of the workload. Serial
+    recurrence: one core."""
+    import numpy as np
+    import oracle
+    chunk = 1 << 24
+    xs = x_cpu[:chunk].astype(np.float64)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        oracle.sosfilt_f64(sos, xs)
+        done += xs.size
+        if time.perf_counter() - t0 >= budget_s or done >= (1 << 28):
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{done} samples (repeated first 2^24 samples of the workload), FP64 cascade, "
+                      f"{dt:.1f} s on one host core"}
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    """Reference arm: the reference's own CPU implementation of the path (its golden
+    generator's FP64 sosfilt cascade, restated in C under oracle/) on the host cores."""
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    from scipy import signal
+    oracle.build()
+    sos = signal.butter(HEADLINE["order"], 0.1, output="sos")
+    sample = 1 << 22  # per step: a bounded sample of the 2^28-sample workload
+    x = np.random.default_rng(1).uniform(-1, 1, sample).astype(np.float64)
+    for _ in range(args.warmup):
+        oracle.sosfilt_f64(sos, x)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.sosfilt_f64(sos, x)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = sample / dt / 1e9
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"butter order {HEADLINE['order']} cutoff 0.1, uniform[-1,1) seed 1; "
+                               f"step = 2^22-sample sample of the 2^{LOG2N}-sample signal",
+                   "n_samples_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{sample} samples per step, FP64 cascade (serial recurrence, one core)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+    import numpy as np
+    import torch
+    from scipy import signal
+
+    import cuda_recursive_filtering_gb300 as pkg
+    from cuda_recursive_filtering_gb300 import Plan, sosfilt, workloads
+
+    torch.cuda.set_device(local_rank)
+    pkg.load_library()
+    dev = torch.device("cuda", local_rank)
+    n = 1 << LOG2N
+    stream = torch.cuda.current_stream()
+    x = workloads.uniform_signal(n, 1, device=dev)
+    y = torch.empty_like(x)
+    pk = peaks()
+
+    # ---- headline: device-resident throughput ----
+    sos = signal.butter(HEADLINE["order"], 0.1, output="sos")
+    plan = Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=n, device=dev)
+    for _ in range(2):
+        plan(x, y)
+    torch.cuda.synchronize()
+    # correctness of this exact run on a prefix (causal filter: first M outputs depend on the
+    # first M inputs only)
+    import oracle
+    m = 1 << 20
+    xp = x[:m].cpu().numpy()
+    _, ref = oracle.reference_golden(sos, xp)
+    chk = oracle.errors(y[:m].cpu().numpy(), ref)
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.15)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    ms = time_plan(plan, x, y, args.steps, args.warmup, stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3) / 1e9
+    achieved = BYTES_PER_SAMPLE * n / (ms * 1e-3) / 1e9
+
+    # ---- end to end: host buffers through the public API (C ABI), copies inside ----
+    e2e = None
+    if rank == 0 or world > 1:
+        xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        xh.copy_(x.cpu())
+        yh = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        xd = torch.empty_like(x)
+        yd = torch.empty_like(x)
+        e2e_steps = max(2, min(args.steps, 5))
+        for _ in range(1):
+            xd.copy_(xh, non_blocking=True)
+            sosfilt(sos, xd, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], out=yd)
+            yh.copy_(yd, non_blocking=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            xd.copy_(xh, non_blocking=True)
+            sosfilt(sos, xd, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], out=yd)
+            yh.copy_(yd, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / e2e_steps
+        e2e = {"value": world * n / dt / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n,
+               "ms_per_step": dt * 1e3}
+        del xh, yh, xd, yd
+
+    # ---- per-order / per-realization rows ----
+    rows = {}
+    if not args.no_sweep:
+        for order in (2, 4, 8, 16):
+            s_o = signal.butter(order, 0.1, output="sos")
+            for kname, (b, nb) in SWEEP_GEOM.items():
+                if kname == "PLR" and order > 8:
+                    continue  # float32 direct form fails the accuracy gate at order 16
+                try:
+                    pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
+                    t = time_plan(pl, x, y, max(3, args.steps // 2), 2, stream)
+                    pl.close()
+                    rows[f"order{order}_{kname}"] = round(n / (t * 1e-3) / 1e9, 1)
+                except Exception as exc:  # report, do not hide
+                    rows[f"order{order}_{kname}"] = f"error: {exc}"
+    if rank != 0:
+        return
+    cpu = cpu_baseline_sample(sos, x[: 1 << 24].cpu().numpy(), budget_s=args.cpu_seconds)
+    traffic = ncu_traffic_per_launch()
+    out = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"plain roofline sweep: butter order {HEADLINE['order']} cutoff 0.1 (SOS), "
+                               f"2^{LOG2N} float32 samples uniform[-1,1) seed 1, zero initial state",
+                   "kernel": HEADLINE["kernel"], "geometry": f"{HEADLINE['block_size']}x{HEADLINE['n_blocks']}",
+                   "n_samples": n, "order": HEADLINE["order"],
+                   "l2": "inputs (1 GiB) larger than L2 (129 MB): no flush between steps",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+                     "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": args.steps * plan.launches_per_execute(),
+        "clocks": clk,
+        "check": {"rel_max": chk["rel_max"], "rel_rms": chk["rel_rms"], "prefix_samples": m},
+        "per_order_gsps": rows,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

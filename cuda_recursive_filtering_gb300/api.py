@@ -103,6 +103,9 @@ class Plan:
         check(st, "iir_plan_execute")
         return out
 
+    def launches_per_execute(self) -> int:
+        return int(self._lib.iir_plan_launches_per_execute(self._ptr))
+
     def check(self, stream=None) -> None:
         """Synchronises the stream and raises IirError if a launch recorded a device error."""
         check(self._lib.iir_plan_check(self._ptr, _stream_handle(stream)), "device")
