@@ -20,6 +20,7 @@ IIR_ERR_CUDA = -3
 IIR_ERR_LOOKBACK_TIMEOUT = -4
 IIR_ERR_OUT_OF_MEMORY = -5
 IIR_ERR_TOO_LARGE = -6
+IIR_NOALLOC_MAX_SAMPLES = 1 << 26
 
 KERNELS = {"AUTO": 0, "PH": 1, "STCR": 2, "STCR_UNROLL": 3, "DTCR": 4, "DTCR_UNROLL": 5, "PLR": 6}
 KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
@@ -54,6 +55,7 @@ def load(path: str | None = None):
     sigs = {
         "iir_sos_filter": ([vp, vp, sz, fp, i, i, vp], i),
         "iir_sos_filter_geom": ([vp, vp, sz, fp, i, i, i, i, vp], i),
+        "iir_sos_filter_noalloc": ([vp, vp, sz, fp, i, vp], i),
         "iir_plan_create": ([pp, fp, i, i, i, i, sz], i),
         "iir_plan_create_plr_ba": ([pp, dp, dp, i, ctypes.c_double, i, i, sz], i),
         "iir_plan_execute": ([vp, vp, vp, sz, vp], i),

@@ -27,12 +27,14 @@
 #include <vector>
 
 #include "../../include/iir_gb300.h"
+#include "iir_host_internal.h"
 #include "iir_params.h"
 #include "iir_registry.h"
 
 using namespace iirgb;
 
-namespace {
+// Planner helpers, shared with iir_noalloc.cu through iir_host_internal.h.
+namespace iirhost {
 
 // ---------------------------------------------------------------------------------------
 // kernel registry
@@ -107,14 +109,9 @@ int ilog2(int v) {
     return l;
 }
 
-struct SectionF32 {
-    float b1, b2, a1, a2;
-};
-
 // Normalises scipy SOS rows {b0,b1,b2,a0,a1,a2} to b0 = a0 = 1 (FP64), returns the removed
 // gain prod(b0/a0). Reference convention: ph_kernels.cuh:157-161, tools/ref_generate.py:62-67.
-int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out, double& gain) {
-    out.clear();
+int normalise_sos(const float* sos, int n_sections, SectionF32* out, double& gain) {
     gain = 1.0;
     for (int s = 0; s < n_sections; ++s) {
         const double b0 = sos[6 * s + 0], b1 = sos[6 * s + 1], b2 = sos[6 * s + 2];
@@ -125,10 +122,17 @@ int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out
         if (a0 == 0.0) return IIR_ERR_INVALID_ARGUMENT;
         if (b0 == 0.0) return IIR_ERR_UNSUPPORTED;  // section gain cannot be factored out
         gain *= b0 / a0;
-        out.push_back(SectionF32{static_cast<float>(b1 / b0), static_cast<float>(b2 / b0),
-                                 static_cast<float>(-a1 / a0), static_cast<float>(-a2 / a0)});
+        out[s] = SectionF32{static_cast<float>(b1 / b0), static_cast<float>(b2 / b0), static_cast<float>(-a1 / a0),
+                            static_cast<float>(-a2 / a0)};
     }
     return IIR_OK;
+}
+
+int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out, double& gain) {
+    out.assign(static_cast<size_t>(n_sections), SectionF32{});
+    const int st = normalise_sos(sos, n_sections, out.data(), gain);
+    if (st) out.clear();
+    return st;
 }
 
 // Fills one IirSection and its lane tables for geometry B x N.
@@ -246,7 +250,9 @@ int cuda_status(cudaError_t e) {
     return e == cudaErrorMemoryAllocation ? IIR_ERR_OUT_OF_MEMORY : IIR_ERR_CUDA;
 }
 
-}  // namespace
+}  // namespace iirhost
+
+using namespace iirhost;
 
 // -------------------------------------------------------------------------------------------
 // plan

@@ -1,0 +1,32 @@
+// iir_host_internal.h — planner helpers defined in iir_host.cu and used by the other host
+// translation units of the library (not part of the C ABI).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "iir_params.h"
+#include "iir_registry.h"
+
+namespace iirhost {
+
+struct SectionF32 {
+    float b1, b2, a1, a2;
+};
+
+// Registered kernel for (realization, B, N, order); nullptr if none.
+const iirgb::KernelEntry* find_entry(int kind, int B, int N, int order);
+// Resident blocks per SM for a registered kernel; also sets its dynamic shared memory limit.
+int blocks_per_sm(const iirgb::KernelEntry& e, int device);
+// scipy SOS rows -> b0 = a0 = 1 sections (FP64 division, float32 result) and the gain.
+int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out, double& gain);
+int normalise_sos(const float* sos, int n_sections, SectionF32* out, double& gain);  // out[n_sections]
+// One section's kernel coefficients and its IIR_TAB_STRIDE lane-table entries.
+int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSection& q, float4* tab);
+// 2D tensor map over a float32 signal viewed as 128-byte lines, box = lines_per_block lines.
+bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int lines_per_block);
+// cudaError_t -> IIR_* status (clears the runtime's sticky last error).
+int cuda_status(cudaError_t e);
+
+}  // namespace iirhost

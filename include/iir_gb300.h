@@ -78,6 +78,22 @@ int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_s
 int iir_sos_filter_geom(const float* x, float* y, size_t n, const float* sos, int n_sections,
                         int kernel, int block_size, int n_blocks, void* stream);
 
+/* Filtering that allocates nothing (no counterpart in the reference, whose callers allocate
+ * the status and carry buffers themselves, src/test_accuracy.cu:136-147). For callers that
+ * must not allocate while they filter: cudaMalloc / cudaFree may synchronise the device and
+ * may fail under memory pressure, which a real-time caller (an audio or radio callback with a
+ * deadline) or a caller whose device memory belongs to another allocator cannot accept.
+ * Runs the PH realization (32 x 64) on one fixed static device array (about 2.2 MB per
+ * device) that holds the launch state, the lane tables and the carry slots.
+ *   - n <= IIR_NOALLOC_MAX_SAMPLES, else IIR_ERR_TOO_LARGE; 1 <= n_sections <= 8.
+ *   - The first call on a device sets the array up (resolves its address, zeroes it,
+ *     synchronises the device); make it before any stream capture.
+ *   - Every call on a device shares the array: calls must be ordered (one stream, or
+ *     streams ordered by events). Calls that overlap in time race and give wrong output. */
+#define IIR_NOALLOC_MAX_SAMPLES (1ull << 26)
+int iir_sos_filter_noalloc(const float* x, float* y, size_t n, const float* sos, int n_sections,
+                           void* stream);
+
 /* ---- plan API (reference: setup_kernel_coefficients + the caller-owned buffers) ---- */
 
 /* Creates a plan on the current CUDA device. The status/carry buffers are sized for

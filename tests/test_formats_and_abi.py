@@ -59,6 +59,13 @@ def test_library_exports_every_declared_symbol(built_library):
         assert f" T {n}" in nm, n
 
 
+def test_noalloc_limit_matches_header():
+    import re
+    text = open(_lib.HEADER).read()
+    m = re.search(r"#define IIR_NOALLOC_MAX_SAMPLES \(1ull << (\d+)\)", text)
+    assert m and (1 << int(m.group(1))) == _lib.IIR_NOALLOC_MAX_SAMPLES
+
+
 def test_status_strings_and_argument_checks(built_library):
     L = _lib.load(built_library)
     assert L.iir_version() >= 10000
