@@ -32,8 +32,8 @@ METRIC = "GS/s (fp32 samples per second through the cascaded-biquad filter)"
 UNIT = "GS/s"
 LOG2N = 28
 HEADLINE = {"kernel": "DTCR_UNROLL", "order": 2, "block_size": 32, "n_blocks": 64}
-SWEEP_GEOM = {"PH": (32, 64), "STCR": (32, 64), "STCR_UNROLL": (32, 64), "DTCR": (32, 64),
-              "DTCR_UNROLL": (32, 64), "PLR": (0, 0)}
+SWEEP_GEOM = {"PH": [(32, 32), (32, 64)], "STCR": [(32, 32), (32, 64)], "STCR_UNROLL": [(32, 32), (32, 64)],
+              "DTCR": [(32, 32), (32, 64)], "DTCR_UNROLL": [(32, 32), (32, 64)], "PLR": [(0, 0)]}
 BYTES_PER_SAMPLE = 8  # 4 read + 4 written (algorithmic)
 
 
@@ -49,7 +49,7 @@ def peaks() -> dict:
 def ncu_traffic_per_launch() -> float | None:
     """DRAM bytes (read + write) per launch of the headline kernel from the committed ncu
     summary, scaled to 2^28 samples (the summary records bytes per sample)."""
-    path = os.path.join(ROOT, "profiles", "dtcr_order2_traffic.txt")
+    path = os.path.join(ROOT, "profiles", "dtcr_unroll_pipe_order2_full.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -260,16 +260,18 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     if not args.no_sweep:
         for order in (2, 4, 8, 16):
             s_o = signal.butter(order, 0.1, output="sos")
-            for kname, (b, nb) in SWEEP_GEOM.items():
+            for kname, geoms in SWEEP_GEOM.items():
                 if kname == "PLR" and order > 8:
                     continue  # float32 direct form fails the accuracy gate at order 16
-                try:
-                    pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
-                    t = time_plan(pl, x, y, max(3, args.steps // 2), 2, stream)
-                    pl.close()
-                    rows[f"order{order}_{kname}"] = round(n / (t * 1e-3) / 1e9, 1)
-                except Exception as exc:  # report, do not hide
-                    rows[f"order{order}_{kname}"] = f"error: {exc}"
+                for b, nb in geoms:
+                    key = f"order{order}_{kname}" + (f"_{b}x{nb}" if b else "")
+                    try:
+                        pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
+                        t = time_plan(pl, x, y, max(3, args.steps // 2), 2, stream)
+                        pl.close()
+                        rows[key] = round(n / (t * 1e-3) / 1e9, 1)
+                    except Exception as exc:  # report, do not hide
+                        rows[key] = f"error: {exc}"
     if rank != 0:
         return
     cpu = cpu_baseline_sample(sos, x[: 1 << 24].cpu().numpy(), budget_s=args.cpu_seconds)
@@ -305,7 +307,10 @@ def main() -> None:
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--log2n", type=int, default=LOG2N,
+                    help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
     args = ap.parse_args()
+    globals()["LOG2N"] = args.log2n
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -28,6 +28,7 @@
 // kernels). Both execute the same operations in the same order, so they are bit-identical.
 #pragma once
 #include "iir_device.cuh"
+#include "iir_pipe.cuh"
 
 namespace iirgb {
 
@@ -118,6 +119,153 @@ struct CrBlock {
         return rl > 0 ? o : 0.f;
     }
 
+    // Zero-padded tile solve of one section for this thread's row (parity halves): FIR +
+    // first double-sided round, elimination levels, top-level scan across the tile's rows,
+    // back-substitution. (P0, P1) = the tile's zero-state end pair (valid in its last row).
+    // Xp0/Xp1: the previous section's incoming state (row-0 input history for sec > 0).
+    // h2, h1: the two input samples before the chunk (row 0's history in section 0).
+    __device__ __forceinline__ static void solve_tile(const IirParams& p, const float* buf, const IirSection& q, int sec,
+                                                      float h2, float h1, int r, int rl, int p0, float Xp0,
+                                                      float Xp1, float (&u)[NPAR][M], float& P0, float& P1) {
+        float s0[NPAR], s1[NPAR];
+        // ---- FIR + first double-sided round -> u (own parity halves) ----
+        const float g = (sec == 0) ? p.gain : 1.f;
+        float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
+        if (r > 0) {
+            x4 = buf[swz<N>(r - 1, N - 4)] * g;
+            x3 = buf[swz<N>(r - 1, N - 3)] * g;
+            x2 = buf[swz<N>(r - 1, N - 2)] * g;
+            x1 = buf[swz<N>(r - 1, N - 1)] * g;
+        } else if (sec == 0) {
+            x4 = x3 = 0.f;
+            x2 = h2 * g;
+            x1 = h1 * g;
+        } else {
+            x4 = x3 = 0.f;
+            x2 = Xp0;
+            x1 = Xp1;
+        }
+        const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
+        // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
+        float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
+        float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+#pragma unroll
+        for (int j = 0; j < N / 4; ++j) {
+            const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+            const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int n = 4 * j + k;
+                const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
+                const int par = n & 1;
+                if (SPLIT) {
+                    if (par == p0) u[0][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                } else {
+                    u[par][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                }
+                x2 = x1;
+                x1 = xs[k];
+                w2 = w1;
+                w1 = wn;
+            }
+        }
+        // ---- elimination levels 1 .. L-1 (previous row's kept tail by shuffle) ----
+#pragma unroll(UNROLL ? 8 : 1)
+        for (int k = 1; k < L; ++k) {
+            const int h = 1 << (k - 1);
+#pragma unroll
+            for (int hh = 0; hh < NPAR; ++hh) {
+                const float prev = prev_row(u[hh][M - 1], rl);
+                Half::eliminate(u[hh], h, q.cr_r[k], q.cr_e[k], prev);
+            }
+        }
+        // ---- top level across the tile's rows: Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t ----
+#pragma unroll
+        for (int hh = 0; hh < NPAR; ++hh) {
+            s0[hh] = 0.f;
+            s1[hh] = u[hh][M - 1];
+            warp_scan2<RW, TPR>(s0[hh], s1[hh], q.M, rl);
+            u[hh][M - 1] = s1[hh];
+        }
+        // ---- back-substitution L-1 .. 1 (zero-padded tile) ----
+#pragma unroll(UNROLL ? 8 : 1)
+        for (int k = L - 1; k >= 1; --k) {
+            const int h = 1 << (k - 1);
+#pragma unroll
+            for (int hh = 0; hh < NPAR; ++hh) {
+                // y at half position -1 - 2h: previous row's, or two rows back at the top
+                const float far = prev_row((2 * h == M) ? s0[hh] : u[hh][M - 1 - 2 * h], rl);
+                Half::backsub(u[hh], h, q.cr_c[k], q.cr_d[k], s0[hh], far);
+            }
+        }
+        // tile end pair (y[N-2], y[N-1]) of the last row
+        if (SPLIT) {
+            const float mine = u[0][M - 1];
+            const float other = __shfl_xor_sync(FULL_MASK, mine, 1);
+            P0 = p0 ? other : mine;
+            P1 = p0 ? mine : other;
+        } else {
+            P0 = u[0][M - 1];
+            P1 = u[1][M - 1];
+        }
+    }
+
+    // u += response of the section recurrence to the row's incoming pair (d2, d1) =
+    // (delta[-2], delta[-1]). DTCR: each parity runs the stride-2 recurrence of its half.
+    __device__ __forceinline__ static void add_response(float (&u)[NPAR][M], const IirSection& q, int p0, float d2,
+                                                        float d1) {
+        const float a1 = q.a1, a2 = q.a2;
+        if (SPLIT) {
+            // stride-2 recurrence of this parity: delta[2m+p] from (delta[p], delta[p+2])
+            const float e0s = fmaf(a1, d1, a2 * d2);    // delta[0]
+            const float e1s = fmaf(a1, e0s, a2 * d1);   // delta[1]
+            const float e2s = fmaf(a1, e1s, a2 * e0s);  // delta[2]
+            const float e3s = fmaf(a1, e2s, a2 * e1s);  // delta[3]
+            float dm2 = p0 ? e1s : e0s, dm1 = p0 ? e3s : e2s;
+            const float al1 = q.ha1, al2 = q.ha2;  // -e_1, -f_1
+            u[0][0] += dm2;
+            u[0][1] += dm1;
+#pragma unroll(UNROLL ? 64 : 1)
+            for (int m = 2; m < M; ++m) {
+                const float dn = fmaf(al1, dm1, al2 * dm2);
+                dm2 = dm1;
+                dm1 = dn;
+                u[0][m] += dn;
+            }
+        } else {
+#pragma unroll
+            for (int n = 0; n < N; ++n) {
+                const float dn = fmaf(a1, d1, a2 * d2);
+                d2 = d1;
+                d1 = dn;
+                u[n & 1][n >> 1] += dn;
+            }
+        }
+    }
+
+    // Row r from this thread's halves into the swizzled buffer (DTCR: float2 pairs (2m, 2m+1),
+    // even m written by parity 0, odd m by parity 1, exchanging values with the partner lane).
+    __device__ __forceinline__ static void write_row(float* buf, const float (&u)[NPAR][M], int r, int p0) {
+        if (SPLIT) {
+#pragma unroll(UNROLL ? 64 : 1)
+            for (int m = 0; m < M; m += 2) {
+                const float a = u[0][m], b = u[0][m + 1];
+                const float oa = __shfl_xor_sync(FULL_MASK, a, 1);
+                const float ob = __shfl_xor_sync(FULL_MASK, b, 1);
+                // parity 0 holds even samples: pair for m is (a, oa); parity 1's for m+1 is (ob, b)
+                if (p0 == 0)
+                    *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m)) = make_float2(a, oa);
+                else
+                    *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m + 2)) = make_float2(ob, b);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < N / 4; ++j)
+                *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j)) =
+                    make_float4(u[0][2 * j], u[1][2 * j], u[0][2 * j + 1], u[1][2 * j + 1]);
+        }
+    }
+
     __device__ static bool filter_block(const IirParams& p, float* buf, BlockAux* aux, uint32_t c, uint32_t epoch,
                                         int warp, int lane) {
         const bool row_warp = warp > 0;
@@ -127,98 +275,19 @@ struct CrBlock {
         const int p0 = SPLIT ? (lane & 1) : 0;        // first parity handled
         float u[NPAR][M];
         float Xp0 = 0.f, Xp1 = 0.f;  // previous section's incoming state (row-0 input history)
+        float h2 = 0.f, h1 = 0.f;    // input samples before the chunk
+        if (row_warp && r == 0 && c > 0) {
+            const long long cs = static_cast<long long>(c) * (ROWS * N);
+            h2 = __ldg(p.x + cs - 2);
+            h1 = __ldg(p.x + cs - 1);
+        }
         for (int sec = 0; sec < p.n_sections; ++sec) {
             const IirSection& q = p.sec[sec];
             const float4* tab = p.tables + sec * IIR_TAB_STRIDE;
             const float4 Ct = tab[IIR_TAB_CPOW + RW - 1];  // tile transition C^RW
-            float s0[NPAR], s1[NPAR];
             float P0 = 0.f, P1 = 0.f;  // tile zero-state end pair (valid in the tile's last row)
             if (row_warp) {
-                // ---- FIR + first double-sided round -> u (own parity halves) ----
-                const float g = (sec == 0) ? p.gain : 1.f;
-                float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
-                if (r > 0) {
-                    x4 = buf[swz<N>(r - 1, N - 4)] * g;
-                    x3 = buf[swz<N>(r - 1, N - 3)] * g;
-                    x2 = buf[swz<N>(r - 1, N - 2)] * g;
-                    x1 = buf[swz<N>(r - 1, N - 1)] * g;
-                } else if (sec == 0) {
-                    x4 = x3 = 0.f;
-                    if (c > 0) {
-                        const long long cs = static_cast<long long>(c) * (ROWS * N);
-                        x2 = __ldg(p.x + cs - 2) * g;
-                        x1 = __ldg(p.x + cs - 1) * g;
-                    } else {
-                        x2 = x1 = 0.f;
-                    }
-                } else {
-                    x4 = x3 = 0.f;
-                    x2 = Xp0;
-                    x1 = Xp1;
-                }
-                const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
-                // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
-                float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
-                float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
-#pragma unroll
-                for (int j = 0; j < N / 4; ++j) {
-                    const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
-                    const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int n = 4 * j + k;
-                        const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
-                        const int par = n & 1;
-                        if (SPLIT) {
-                            if (par == p0) u[0][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
-                        } else {
-                            u[par][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
-                        }
-                        x2 = x1;
-                        x1 = xs[k];
-                        w2 = w1;
-                        w1 = wn;
-                    }
-                }
-                // ---- elimination levels 1 .. L-1 (previous row's kept tail by shuffle) ----
-#pragma unroll(UNROLL ? 8 : 1)
-                for (int k = 1; k < L; ++k) {
-                    const int h = 1 << (k - 1);
-#pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) {
-                        const float prev = prev_row(u[hh][M - 1], rl);
-                        Half::eliminate(u[hh], h, q.cr_r[k], q.cr_e[k], prev);
-                    }
-                }
-                // ---- top level across the tile's rows: Y_t + e_L Y_{t-1} + f_L Y_{t-2} = V_t ----
-#pragma unroll
-                for (int hh = 0; hh < NPAR; ++hh) {
-                    s0[hh] = 0.f;
-                    s1[hh] = u[hh][M - 1];
-                    warp_scan2<RW, TPR>(s0[hh], s1[hh], q.M, rl);
-                    u[hh][M - 1] = s1[hh];
-                }
-                // ---- back-substitution L-1 .. 1 (zero-padded tile) ----
-#pragma unroll(UNROLL ? 8 : 1)
-                for (int k = L - 1; k >= 1; --k) {
-                    const int h = 1 << (k - 1);
-#pragma unroll
-                    for (int hh = 0; hh < NPAR; ++hh) {
-                        // y at half position -1 - 2h: previous row's, or two rows back at the top
-                        const float far = prev_row((2 * h == M) ? s0[hh] : u[hh][M - 1 - 2 * h], rl);
-                        Half::backsub(u[hh], h, q.cr_c[k], q.cr_d[k], s0[hh], far);
-                    }
-                }
-                // tile end pair (y[N-2], y[N-1]) of the last row
-                if (SPLIT) {
-                    const float mine = u[0][M - 1];
-                    const float other = __shfl_xor_sync(FULL_MASK, mine, 1);
-                    P0 = p0 ? other : mine;
-                    P1 = p0 ? mine : other;
-                } else {
-                    P0 = u[0][M - 1];
-                    P1 = u[1][M - 1];
-                }
+                solve_tile(p, buf, q, sec, h2, h1, r, rl, p0, Xp0, Xp1, u, P0, P1);
                 if (lane == 31) {
                     aux->wtot[w][0][0] = P0;
                     aux->wtot[w][0][1] = P1;
@@ -245,49 +314,8 @@ struct CrBlock {
                 }
                 float d2 = S0, d1 = S1;  // (delta[-2], delta[-1]) at the row start
                 if (rl > 0) mv2(tab[IIR_TAB_CPOW + rl - 1], S0, S1, d2, d1);
-                const float a1 = q.a1, a2 = q.a2;
-                if (SPLIT) {
-                    // stride-2 recurrence of this parity: delta[2m+p] from (delta[p], delta[p+2])
-                    const float e0s = fmaf(a1, d1, a2 * d2);    // delta[0]
-                    const float e1s = fmaf(a1, e0s, a2 * d1);   // delta[1]
-                    const float e2s = fmaf(a1, e1s, a2 * e0s);  // delta[2]
-                    const float e3s = fmaf(a1, e2s, a2 * e1s);  // delta[3]
-                    float dm2 = p0 ? e1s : e0s, dm1 = p0 ? e3s : e2s;
-                    const float al1 = q.ha1, al2 = q.ha2;  // -e_1, -f_1
-                    u[0][0] += dm2;
-                    u[0][1] += dm1;
-#pragma unroll(UNROLL ? 64 : 1)
-                    for (int m = 2; m < M; ++m) {
-                        const float dn = fmaf(al1, dm1, al2 * dm2);
-                        dm2 = dm1;
-                        dm1 = dn;
-                        u[0][m] += dn;
-                    }
-                    // write the row as float2 pairs (2m, 2m+1): even m by parity 0, odd m by parity 1
-#pragma unroll(UNROLL ? 64 : 1)
-                    for (int m = 0; m < M; m += 2) {
-                        const float a = u[0][m], b = u[0][m + 1];
-                        const float oa = __shfl_xor_sync(FULL_MASK, a, 1);
-                        const float ob = __shfl_xor_sync(FULL_MASK, b, 1);
-                        // parity 0 holds even samples: pair for m is (a, oa); parity 1's for m+1 is (ob, b)
-                        if (p0 == 0)
-                            *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m)) = make_float2(a, oa);
-                        else
-                            *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m + 2)) = make_float2(ob, b);
-                    }
-                } else {
-#pragma unroll
-                    for (int n = 0; n < N; ++n) {
-                        const float dn = fmaf(a1, d1, a2 * d2);
-                        d2 = d1;
-                        d1 = dn;
-                        u[n & 1][n >> 1] += dn;
-                    }
-#pragma unroll
-                    for (int j = 0; j < N / 4; ++j)
-                        *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j)) =
-                            make_float4(u[0][2 * j], u[1][2 * j], u[0][2 * j + 1], u[1][2 * j + 1]);
-                }
+                add_response(u, q, p0, d2, d1);
+                write_row(buf, u, r, p0);
                 Xp0 = X0;
                 Xp1 = X1;
                 named_barrier_rows(NW);  // rows written before the next section reads histories
@@ -295,6 +323,94 @@ struct CrBlock {
         }
         if (row_warp) fence_proxy_async_smem();
         return true;
+    }
+};
+
+
+// Single-section STCR / DTCR on the persistent pipeline (iir_pipe.cuh). P1 = the tile solve
+// of CrBlock (zero-state rows written back to the stage), the per-tile zero-state incoming
+// pairs and the chunk aggregate; P2 = the correction by the response to the chunk's incoming
+// state. The same float operations as CrBlock::filter_block, so the output is bit-identical
+// to the one-block-per-chunk schedule.
+template <bool SPLIT, int N_, int ROWS_, bool UNROLL>
+struct CrPipe {
+    using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL>;
+    static constexpr int N = N_, ROWS = ROWS_, M = Blk::M, NPAR = Blk::NPAR, RW = Blk::RW, NW = Blk::NW;
+
+    __device__ __forceinline__ static void geometry(int w, int lane, int& rl, int& r, int& p0) {
+        rl = SPLIT ? (lane >> 1) : lane;
+        r = w * RW + rl;
+        p0 = SPLIT ? (lane & 1) : 0;
+    }
+
+    __device__ static void p1(const IirParams& p, float* buf, const float* hist, const float4* tc, float (*zin)[2],
+                              PipeAux* aux, int slot, uint32_t, int w, int lane) {
+        int rl, r, p0;
+        geometry(w, lane, rl, r, p0);
+        const IirSection& q = p.sec[0];
+        const float4 Ct = tc[RW - 1];  // C^RW
+        float u[NPAR][M];
+        float P0, P1;
+        Blk::solve_tile(p, buf, q, 0, hist[30], hist[31], r, rl, p0, 0.f, 0.f, u, P0, P1);
+        if (lane == 31) {
+            aux->wtot[w][0][0] = P0;
+            aux->wtot[w][0][1] = P1;
+        }
+        named_barrier_rows(NW);  // every row read its input history; tile end pairs visible
+        Blk::write_row(buf, u, r, p0);
+        float in0, in1;
+        warp_incoming(aux, w, 0, Ct, in0, in1);
+        if (lane == 0) {
+            zin[w][0] = in0;
+            zin[w][1] = in1;
+        }
+        if (w == NW - 1 && lane == 31) {
+            // chunk aggregate = C^RW (incoming of the last tile) + its end pair
+            float n0, n1;
+            mv2(Ct, in0, in1, n0, n1);
+            aux->partv[slot][0] = n0 + P0;
+            aux->partv[slot][1] = n1 + P1;
+        }
+    }
+
+    __device__ static void p2(const IirParams& p, float* buf, const float4* tc, const float (*zin)[2], float X0,
+                              float X1, uint32_t, int w, int lane) {
+        int rl, r, p0;
+        geometry(w, lane, rl, r, p0);
+        const IirSection& q = p.sec[0];
+        float S0 = X0, S1 = X1;
+        if (w > 0) {
+            float t0, t1;
+            mv2(tc[RW * w - 1], X0, X1, t0, t1);  // C^(RW w)
+            S0 = t0 + zin[w][0];
+            S1 = t1 + zin[w][1];
+        }
+        float d2 = S0, d1 = S1;
+        if (rl > 0) mv2(tc[rl - 1], S0, S1, d2, d1);  // C^rl
+        // In place on the row: STCR runs the response over the whole row; DTCR's two lanes
+        // take the row's two contiguous halves (A^(N/2) moves the incoming pair to the middle).
+        constexpr int SPAN = SPLIT ? N / 2 : N;
+        if (SPLIT && p0) {
+            float h2, h1;
+            mv2(tc[PipeGeom<ROWS, N, 2>::TC_HALF], d2, d1, h2, h1);
+            d2 = h2;
+            d1 = h1;
+        }
+        const int n0 = SPLIT ? p0 * (N / 2) : 0;
+#pragma unroll 4
+        for (int j = 0; j < SPAN / 4; ++j) {
+            float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, n0 + 4 * j));
+            const float4 v = *ptr;
+            float o[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float dn = fmaf(q.a1, d1, q.a2 * d2);
+                d2 = d1;
+                d1 = dn;
+                o[k] += dn;
+            }
+            *ptr = make_float4(o[0], o[1], o[2], o[3]);
+        }
     }
 };
 

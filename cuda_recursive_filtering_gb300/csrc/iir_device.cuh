@@ -130,11 +130,10 @@ __device__ __forceinline__ uint32_t take_ticket(IirLaunchState* st, uint32_t nch
     return c;
 }
 
-// Short busy back-off between polls (cycles, doubling up to a cap).
+// Short back-off between polls (about `cycles` / 2 ns, doubling up to a cap). The warp
+// sleeps rather than spins, so it takes no issue slots from the warps that compute.
 __device__ __forceinline__ void backoff(uint32_t& cycles) {
-    const long long t0 = clock64();
-    while (clock64() - t0 < cycles) {
-    }
+    __nanosleep(cycles >> 1);
     if (cycles < 1024u) cycles <<= 1;
 }
 
@@ -595,7 +594,8 @@ __device__ __forceinline__ bool control_section(const P& p, BlockAux* aux, int s
 }
 
 // Row warps: zero-state incoming state of warp `w` (row-warp index) for scan q.
-__device__ __forceinline__ void warp_incoming(const BlockAux* aux, int w, int q, float4 Gw, float& i0, float& i1) {
+template <class Aux>
+__device__ __forceinline__ void warp_incoming(const Aux* aux, int w, int q, float4 Gw, float& i0, float& i1) {
     i0 = 0.f;
     i1 = 0.f;
     for (int v = 0; v < w; ++v) {

@@ -51,10 +51,21 @@ std::vector<KernelEntry>& registry() {
     return reg;
 }
 
-const KernelEntry* find_entry(int kind, int B, int N, int order) {
+const KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline) {
     for (const KernelEntry& e : registry())
-        if (e.kind == kind && e.B == B && e.N == N && e.order == order) return &e;
+        if (e.kind == kind && e.B == B && e.N == N && e.order == order && e.pipeline == pipeline) return &e;
     return nullptr;
+}
+
+// Schedule of single-section filters: the persistent pipeline where one is registered for
+// the realization and geometry, unless IIR_GB300_SCHEDULE=ticket asks for the one-block-per-
+// chunk kernel (kept for comparison).
+bool pipeline_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("IIR_GB300_SCHEDULE");
+        return !(v && std::strcmp(v, "ticket") == 0);
+    }();
+    return on;
 }
 
 struct OccKey {
@@ -210,6 +221,7 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
         Pq = mmul(Pq, Qg);
     }
     for (int l = IIR_TAB_QG + 33; l < IIR_TAB_STRIDE; ++l) tab[l] = make_float4(0, 0, 0, 0);
+    tab[IIR_TAB_HALF] = to_f4(mpow(A, static_cast<unsigned long long>(N / 2)));
     return IIR_OK;
 }
 
@@ -244,6 +256,20 @@ bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int line
     return r == CUDA_SUCCESS;
 }
 
+// Same view with a one-line box and no swizzle: the 32 samples before a chunk.
+bool encode_hist_map(CUtensorMap* map, const float* base, long long n) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || n < 32 || (reinterpret_cast<uintptr_t>(base) & 15u)) return false;
+    const cuuint64_t dims[2] = {32ull, static_cast<cuuint64_t>(n / 32)};
+    const cuuint64_t strides[1] = {128ull};
+    const cuuint32_t box[2] = {32u, 1u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 int cuda_status(cudaError_t e) {
     if (e == cudaSuccess) return IIR_OK;
     cudaGetLastError();
@@ -271,6 +297,7 @@ struct iir_plan {
     size_t carry_cap = 0;      // chunks
     float4* d_tables = nullptr;
     float* d_fac = nullptr;    // PLR factor arrays
+    float4* d_qpow = nullptr;  // persistent pipeline: chunk transition powers Q^t, t < grid_max
     IirParams params{};
     IirPlrParams plr{};
     long long timeout_ns = 1000000000ll;
@@ -352,6 +379,7 @@ void plan_free(iir_plan* p) {
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_fac) cudaFree(p->d_fac);
+    if (p->d_qpow) cudaFree(p->d_qpow);
     delete p;
 }
 
@@ -508,7 +536,9 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     }
     int B = block_size, N = n_blocks;
     default_geometry(kernel, n_sections, B, N);
-    const KernelEntry* e = find_entry(kernel, B, N, 0);
+    const KernelEntry* e = nullptr;
+    if (n_sections == 1 && pipeline_enabled()) e = find_entry(kernel, B, N, 0, 1);
+    if (!e) e = find_entry(kernel, B, N, 0, 0);
     if (!e) return IIR_ERR_UNSUPPORTED;
     iir_plan* p = new iir_plan();
     p->kind = kernel;
@@ -530,6 +560,21 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     if (!st) st = cuda_status(cudaMalloc(&p->d_tables, tabs.size() * sizeof(float4)));
     if (!st)
         st = cuda_status(cudaMemcpy(p->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (!st && e->pipeline) {
+        // Q^t (FP64, rounded once) for the windowed lookback of the persistent pipeline
+        const M2 A{0.0, 1.0, static_cast<double>(secs[0].a2), static_cast<double>(secs[0].a1)};
+        const M2 Q = mpow(mpow(A, static_cast<unsigned long long>(N)), static_cast<unsigned long long>(e->rows));
+        std::vector<float4> qp(static_cast<size_t>(p->grid_max));
+        M2 P{1, 0, 0, 1};
+        for (int t = 0; t < p->grid_max; ++t) {
+            qp[t] = to_f4(P);
+            P = mmul(P, Q);
+        }
+        st = cuda_status(cudaMalloc(&p->d_qpow, qp.size() * sizeof(float4)));
+        if (!st) st = cuda_status(cudaMemcpy(p->d_qpow, qp.data(), qp.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        q.qpow = p->d_qpow;
+        q.qpow_len = static_cast<unsigned int>(p->grid_max);
+    }
     if (st) {
         plan_free(p);
         return st;
@@ -600,13 +645,21 @@ int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stre
         q.carry_stride = carry_words_per_section(p, p->carry_cap);
         const int lines = static_cast<int>(chunk / 32);
         q.use_tma = (aligned && encode_lines_map(&q.tmap_x, x, static_cast<long long>(n), lines) &&
-                     encode_lines_map(&q.tmap_y, y, static_cast<long long>(n), lines))
+                     encode_lines_map(&q.tmap_y, y, static_cast<long long>(n), lines) &&
+                     (!p->entry->pipeline || encode_hist_map(&q.tmap_h, x, static_cast<long long>(n))))
                         ? 1
                         : 0;
         q.timeout_ns = p->timeout_ns;
         q.withhold_chunk = p->withhold;
         void* args[] = {&q};
-        err = cudaLaunchKernel(p->entry->fn, dim3(grid), dim3(p->entry->threads), args, p->entry->smem, stream);
+        if (p->entry->pipeline) {
+            // persistent: at most every resident block, all co-resident (cooperative launch)
+            const int pgrid = static_cast<int>(std::min<size_t>(nchunks, static_cast<size_t>(p->grid_max)));
+            err = cudaLaunchCooperativeKernel(p->entry->fn, dim3(pgrid), dim3(p->entry->threads), args,
+                                              p->entry->smem, stream);
+        } else {
+            err = cudaLaunchKernel(p->entry->fn, dim3(grid), dim3(p->entry->threads), args, p->entry->smem, stream);
+        }
     }
     p->withhold = -1;  // one launch only
     return cuda_status(err);

@@ -20,11 +20,13 @@
 //                                 companion for STCR / DTCR), t < 32 rows per warp
 //   [TAB_QC + l]   = Q^l,      Q = A^(rows*N) (chunk transition), l <= 32
 //   [TAB_QG + l]   = Q^(32 l)  (group transition powers), l <= 32
+//   [TAB_HALF]     = A^(N/2)   (half-row transition)
 #define IIR_GROUP 32
 #define IIR_TAB_CPOW 0
 #define IIR_TAB_GPOW 256
 #define IIR_TAB_QC 288
 #define IIR_TAB_QG 321
+#define IIR_TAB_HALF 354
 #define IIR_TAB_STRIDE 356
 
 // Device-side per-plan launch state. `ticket` packs the launch epoch (the reference's
@@ -37,7 +39,9 @@
 struct IirLaunchState {
     unsigned long long ticket;       // (epoch << 32) | ticket
     unsigned long long error;        // (epoch << 32) | status code of the first failure
-    unsigned long long pad[2];
+    unsigned int done;               // persistent kernels: blocks of the launch that have exited
+    unsigned int pad0;
+    unsigned long long pad[1];
 };
 
 struct IirSection {
@@ -56,6 +60,7 @@ struct IirSection {
 struct IirParams {
     CUtensorMap tmap_x;               // 2D view of x as 32-float lines, 128B swizzle (bulk path)
     CUtensorMap tmap_y;
+    CUtensorMap tmap_h;               // persistent pipeline: one 32-float line, no swizzle (input history)
     const float* x;
     float* y;
     long long n;
@@ -72,6 +77,9 @@ struct IirParams {
     float gain;
     int pad0;
     unsigned long long* prof;         // per-block phase timestamps (IIR_PROFILE builds only)
+    const float4* qpow;               // persistent pipeline: Q^t, t < qpow_len (chunk transition powers)
+    unsigned int qpow_len;
+    int pad1;
     IirSection sec[IIR_MAX_SECTIONS];
 };
 

@@ -26,6 +26,7 @@ struct KernelEntry {
     size_t smem;    // dynamic shared memory bytes
     int order;      // PLR direct-form order (0 for the cascaded realizations)
     int rows;       // rows per block (tiles x B) for the row-major realizations
+    int pipeline = 0;  // 1: single-section persistent pipeline, launched cooperatively
 };
 
 void register_ph(std::vector<KernelEntry>& reg);

@@ -17,8 +17,8 @@ What it produces (all small):
         plr2_{B}_{X}           tools/plr_emulator.py plr_pass(...) (order 2, with a ragged tail)
         direct_{order}         tools/plr_emulator.py direct_form_f32 on 2^12 samples
       plus the matching inputs (x_*) and float64 references (ref_*).
-  baseline_c1.npz
-      BASELINE config 1 (butter(2, 0.1), 2^14 samples of uniform[-1,1] from seed 0) with
+  sosfilt_order2_uniform.npz
+      butter(2, 0.1) on 2^14 samples of uniform[-1,1] from seed 0, with
       scipy.signal.sosfilt's FP64 output, and the scipy version used.
 """
 from __future__ import annotations
@@ -100,13 +100,13 @@ def make_emulators(ref_root: str) -> None:
     np.savez_compressed(os.path.join(HERE, "emulators.npz"), **out)
 
 
-def make_baseline_c1() -> None:
+def make_sosfilt_order2_uniform() -> None:
     import scipy
     from scipy import signal
     sos = signal.butter(2, 0.1, output="sos")
     x = np.random.default_rng(0).uniform(-1.0, 1.0, 1 << 14).astype(np.float32)
     y = signal.sosfilt(sos, x.astype(np.float64))
-    np.savez_compressed(os.path.join(HERE, "baseline_c1.npz"), sos=sos, x=x, y=y,
+    np.savez_compressed(os.path.join(HERE, "sosfilt_order2_uniform.npz"), sos=sos, x=x, y=y,
                         scipy_version=np.array(scipy.__version__))
 
 
@@ -115,7 +115,7 @@ def main() -> None:
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "tools")):
         sys.exit("usage: make_golden.py <reference checkout>")
     make_ref_generate(ref_root)
-    make_baseline_c1()
+    make_sosfilt_order2_uniform()
     make_emulators(ref_root)
 
 

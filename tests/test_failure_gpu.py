@@ -18,9 +18,11 @@ def butter(order, cutoff=0.1):
     return signal.butter(order, cutoff, output="sos")
 
 
-@pytest.mark.parametrize("kernel", ["PH", "DTCR_UNROLL", "STCR", "PLR"])
-def test_withheld_carry_times_out_and_plan_recovers(kernel, cuda_device):
-    sos = butter(4)
+@pytest.mark.parametrize("kernel,order", [("PH", 4), ("PH", 2), ("DTCR_UNROLL", 4), ("DTCR_UNROLL", 2), ("STCR", 4), ("STCR", 2),
+                                          ("PLR", 4)])
+def test_withheld_carry_times_out_and_plan_recovers(kernel, order, cuda_device):
+    """Order 2 runs the single-section persistent pipeline, order 4 the per-chunk blocks."""
+    sos = butter(order)
     n = 1 << 20
     x = np.random.default_rng(0).uniform(-1, 1, n).astype(np.float32)
     xt = torch.from_numpy(x).cuda()

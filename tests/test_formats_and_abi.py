@@ -97,5 +97,5 @@ def test_workload_generators_are_seeded():
     assert np.array_equal(a.numpy(), b.numpy())
     assert float(a.min()) >= -1.0 and float(a.max()) < 1.0
     sos, x = workloads.plain_order2_small(device="cpu")
-    g = np.load(os.path.join(GOLDEN, "baseline_c1.npz"))
+    g = np.load(os.path.join(GOLDEN, "sosfilt_order2_uniform.npz"))
     assert np.array_equal(sos, g["sos"]) and np.array_equal(x.numpy()[: g["x"].size], g["x"])

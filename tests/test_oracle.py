@@ -3,7 +3,7 @@
 Fixtures (tests/golden, made by tests/golden/make_golden.py from the reference's tools):
   ref_order*/reference.bin + filter_taps.hpp   tools/ref_generate.py
   emulators.npz                                tools/{stcr,dtcr,plr}_emulator.py
-  baseline_c1.npz                              scipy.signal.sosfilt, BASELINE config 1
+  sosfilt_order2_uniform.npz                   scipy.signal.sosfilt, butter(2, 0.1) on 2^14 uniform samples
 """
 import os
 
@@ -36,8 +36,8 @@ def test_sosfilt_f64_matches_reference_bin(order):
     assert np.max(np.abs(y.astype(np.float64) - ref)) <= 2e-7 * np.max(np.abs(ref))
 
 
-def test_sosfilt_f64_matches_scipy_baseline_c1():
-    g = np.load(os.path.join(GOLDEN, "baseline_c1.npz"))
+def test_sosfilt_f64_matches_scipy_order2_uniform():
+    g = np.load(os.path.join(GOLDEN, "sosfilt_order2_uniform.npz"))
     y = oracle.sosfilt_f64(g["sos"], g["x"].astype(np.float64))
     assert np.max(np.abs(y - g["y"])) <= 1e-13 * np.max(np.abs(g["y"]))
 

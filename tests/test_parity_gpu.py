@@ -1,7 +1,7 @@
 """GPU parity: every realization x geometry x order against the FP64 oracle (pinned to the
 reference's reference.bin) and against the reference's float32 emulator outputs, through the
 C ABI. Tolerances (written per test): the reference's gate max|err| <= 1e-4 * max|ref|
-(src/test_accuracy.cu:178-188) everywhere it applies, and the benchmark spec's bound
+(src/test_accuracy.cu:178-188) everywhere it applies, and the stated accuracy bound
 max|err| / RMS(ref) <= 1e-5 at orders 2-8 (2e-5 at order 16) for the cascaded realizations.
 """
 import os
@@ -138,8 +138,8 @@ def test_one_shot_api_and_raw_sos(cuda_device):
         assert torch.equal(y, y2) or oracle.errors(y2.cpu().numpy(), golden(sos, x))["rel_max"] <= 1e-4
 
 
-def test_config1_order2(cuda_device):
-    """BASELINE config 1: butter(2, 0.1), 2^16 uniform samples (seed 0), PH and DTCR,
+def test_order2_small_uniform(cuda_device):
+    """butter(2, 0.1) on 2^16 uniform samples (seed 0), PH and DTCR,
     gate max|err|/RMS <= 1e-5 against FP64 sosfilt."""
     from cuda_recursive_filtering_gb300 import workloads
     sos, xt = workloads.plain_order2_small()

@@ -1,0 +1,108 @@
+"""Single-section filters on the persistent pipeline (cooperative grid, TMA warp + lookback
+warp + row warps over shared-memory stages) against the FP64 oracle; run to run bit-identical
+(the windowed lookback adds its terms in a fixed order); and equal, within 1e-6 * max|ref|, to
+the one-block-per-chunk schedule of the same realization (IIR_GB300_SCHEDULE=ticket, run in a
+child process because the schedule is chosen once per process).
+Tolerance: max|err| <= 1e-4 * max|ref| (src/test_accuracy.cu:178-188) and
+max|err| / RMS(ref) <= 1e-5 at order 2.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import ROOT
+from cuda_recursive_filtering_gb300 import Plan
+
+pytestmark = pytest.mark.gpu
+
+PIPE_KERNELS = ["PH", "STCR", "STCR_UNROLL", "DTCR", "DTCR_UNROLL"]
+PIPE_GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
+
+
+def _sos(cutoff=0.1):
+    from scipy import signal
+    return signal.butter(2, cutoff, output="sos")
+
+
+def _check(y, x, sos):
+    _, ref = oracle.reference_golden(sos, x)
+    e = oracle.errors(y, ref)
+    assert e["finite"], e
+    assert e["rel_max"] <= 1e-4, e
+    assert e["rel_rms"] <= 1e-5, e
+
+
+@pytest.mark.parametrize("kernel", PIPE_KERNELS)
+@pytest.mark.parametrize("geom", PIPE_GEOMS, ids=lambda g: f"{g[0]}x{g[1]}")
+def test_pipeline_sizes(kernel, geom, cuda_device):
+    sos = _sos()
+    sizes = [1, 31, 33, 8191, 8192, 8193, 3 * 8192 + 5, 152 * 8192, 152 * 2 * 8192 + 4097, (1 << 22) + 77]
+    plan = Plan(sos, kernel, *geom, max_n=max(sizes))
+    assert plan.info()["n_sections"] == 1
+    rng = np.random.default_rng(5)
+    for n in sizes:
+        x = rng.uniform(-1, 1, n).astype(np.float32)
+        y = plan(torch.from_numpy(x).cuda())
+        plan.check()
+        _check(y.cpu().numpy(), x, sos)
+
+
+@pytest.mark.parametrize("kernel", PIPE_KERNELS)
+def test_pipeline_unaligned_and_repeated(kernel, cuda_device):
+    sos = _sos(0.05)
+    n = (1 << 20) + 3
+    rng = np.random.default_rng(6)
+    x = rng.uniform(-1, 1, n).astype(np.float32)
+    plan = Plan(sos, kernel, max_n=n + 1)
+    base = torch.zeros(n + 1, device="cuda")
+    base[1:] = torch.from_numpy(x).cuda()
+    xu = base[1:]                       # 4-byte offset: element-wise staging for every chunk
+    out = torch.empty(n + 1, device="cuda")[1:]
+    for _ in range(3):
+        plan(xu, out)
+    plan.check()
+    _check(out.cpu().numpy(), x, sos)
+    xt = torch.from_numpy(x).cuda()
+    for i in range(40):                # epochs advance; carry slots are reused without reset
+        y = plan(xt[: n - 1000 * i])
+    plan.check()
+    _check(y.cpu().numpy(), x[: n - 39000], sos)
+
+
+_CHILD = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from cuda_recursive_filtering_gb300 import Plan
+from scipy import signal
+x = np.load(sys.argv[2])
+out = {}
+for k in sys.argv[4].split(","):
+    p = Plan(signal.butter(2, 0.1, output="sos"), k, max_n=x.size)
+    out[k] = p(torch.from_numpy(x).cuda()).cpu().numpy()
+    p.check()
+np.savez(sys.argv[3], **out)
+"""
+
+
+def test_pipeline_deterministic_and_matches_ticket_schedule(tmp_path, cuda_device):
+    n = 77 * 8192 + 1234
+    x = np.random.default_rng(7).uniform(-1, 1, n).astype(np.float32)
+    np.save(tmp_path / "x.npy", x)
+    env = dict(os.environ, IIR_GB300_SCHEDULE="ticket")
+    subprocess.run([sys.executable, "-c", _CHILD, ROOT, str(tmp_path / "x.npy"), str(tmp_path / "t.npz"),
+                    ",".join(PIPE_KERNELS)], env=env, check=True, timeout=600)
+    ref = np.load(tmp_path / "t.npz")
+    xt = torch.from_numpy(x).cuda()
+    for k in PIPE_KERNELS:
+        p = Plan(_sos(), k, max_n=n)
+        y1 = p(xt).cpu().numpy()
+        y2 = p(xt).cpu().numpy()
+        p.check()
+        assert np.array_equal(y1, y2), k
+        scale = float(np.max(np.abs(ref[k])))
+        assert np.max(np.abs(y1 - ref[k])) <= 1e-6 * scale, k
