@@ -49,7 +49,7 @@ def peaks() -> dict:
 def ncu_traffic_per_launch() -> float | None:
     """DRAM bytes (read + write) per launch of the headline kernel from the committed ncu
     summary, scaled to 2^28 samples (the summary records bytes per sample)."""
-    path = os.path.join(ROOT, "profiles", "dtcr_unroll_pipe_order2_full.md")
+    path = os.path.join(ROOT, "profiles", "dtcr_unroll_order2_full.md")
     if not os.path.exists(path):
         return None
     for line in open(path):

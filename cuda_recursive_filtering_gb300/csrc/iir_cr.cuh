@@ -28,7 +28,7 @@
 // kernels). Both execute the same operations in the same order, so they are bit-identical.
 #pragma once
 #include "iir_device.cuh"
-#include "iir_pipe.cuh"
+#include "iir_twopass.cuh"
 
 namespace iirgb {
 
@@ -130,43 +130,81 @@ struct CrBlock {
         float s0[NPAR], s1[NPAR];
         // ---- FIR + first double-sided round -> u (own parity halves) ----
         const float g = (sec == 0) ? p.gain : 1.f;
-        float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
-        if (r > 0) {
-            x4 = buf[swz<N>(r - 1, N - 4)] * g;
-            x3 = buf[swz<N>(r - 1, N - 3)] * g;
-            x2 = buf[swz<N>(r - 1, N - 2)] * g;
-            x1 = buf[swz<N>(r - 1, N - 1)] * g;
-        } else if (sec == 0) {
-            x4 = x3 = 0.f;
-            x2 = h2 * g;
-            x1 = h1 * g;
-        } else {
-            x4 = x3 = 0.f;
-            x2 = Xp0;
-            x1 = Xp1;
-        }
-        const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
-        // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
-        float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
-        float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+        if (SPLIT) {
+            // One lane per parity: v1[n] = g (x[n] + fir5 . (x[n-1], .., x[n-4])) only at its own
+            // parities n = 2m + p0, as six taps over x[2m-4 .. 2m+1] whose coefficients depend on
+            // the lane only (no per-sample selects).
+            float m4, m3, m2, m1;  // raw x[-4], x[-3], x[-2], x[-1] of this row
+            if (r > 0) {
+                m4 = buf[swz<N>(r - 1, N - 4)];
+                m3 = buf[swz<N>(r - 1, N - 3)];
+                m2 = buf[swz<N>(r - 1, N - 2)];
+                m1 = buf[swz<N>(r - 1, N - 1)];
+            } else {
+                m4 = m3 = 0.f;
+                m2 = (sec == 0) ? h2 : Xp0;
+                m1 = (sec == 0) ? h1 : Xp1;
+            }
+            const float c0 = g, c1 = g * q.fir5[0], c2 = g * q.fir5[1], c3 = g * q.fir5[2], c4 = g * q.fir5[3];
+            const float d0 = p0 ? 0.f : c4, d1 = p0 ? c4 : c3, d2 = p0 ? c3 : c2, d3 = p0 ? c2 : c1,
+                        d4 = p0 ? c1 : c0, d5 = p0 ? c0 : 0.f;
+            const float xm2 = m2, xm1 = m1;
+            float xr0 = 0.f, xr1 = 0.f;  // raw x[0], x[1] of the row
 #pragma unroll
-        for (int j = 0; j < N / 4; ++j) {
-            const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
-            const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int n = 4 * j + k;
-                const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
-                const int par = n & 1;
-                if (SPLIT) {
-                    if (par == p0) u[0][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
-                } else {
-                    u[par][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+            for (int j = 0; j < N / 4; ++j) {
+                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+                if (j == 0) {
+                    xr0 = v4.x;
+                    xr1 = v4.y;
                 }
-                x2 = x1;
-                x1 = xs[k];
-                w2 = w1;
-                w1 = wn;
+                u[0][2 * j] = fmaf(d5, v4.y, fmaf(d4, v4.x, fmaf(d3, m1, fmaf(d2, m2, fmaf(d1, m3, d0 * m4)))));
+                u[0][2 * j + 1] = fmaf(d5, v4.w, fmaf(d4, v4.z, fmaf(d3, v4.y, fmaf(d2, v4.x, fmaf(d1, m1, d0 * m2)))));
+                m4 = v4.x;
+                m3 = v4.y;
+                m2 = v4.z;
+                m1 = v4.w;
+            }
+            if (rl == 0) {
+                // zero-padded tile: the FIR output before the tile counts as zero, so
+                // v1[0] = w[0] and v1[1] = w[1] - e w[0]
+                const float w0 = g * fmaf(q.b2, xm2, fmaf(q.b1, xm1, xr0));
+                const float w1 = g * fmaf(q.b2, xm1, fmaf(q.b1, xr0, xr1));
+                u[0][0] = p0 ? fmaf(-q.e0, w0, w1) : w0;
+            }
+        } else {
+            float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
+            if (r > 0) {
+                x4 = buf[swz<N>(r - 1, N - 4)] * g;
+                x3 = buf[swz<N>(r - 1, N - 3)] * g;
+                x2 = buf[swz<N>(r - 1, N - 2)] * g;
+                x1 = buf[swz<N>(r - 1, N - 1)] * g;
+            } else if (sec == 0) {
+                x4 = x3 = 0.f;
+                x2 = h2 * g;
+                x1 = h1 * g;
+            } else {
+                x4 = x3 = 0.f;
+                x2 = Xp0;
+                x1 = Xp1;
+            }
+            const float b1 = q.b1, b2 = q.b2, e = q.e0, f = q.f0;
+            // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
+            float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
+            float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+#pragma unroll
+            for (int j = 0; j < N / 4; ++j) {
+                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+                const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int n = 4 * j + k;
+                    const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
+                    u[n & 1][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                    x2 = x1;
+                    x1 = xs[k];
+                    w2 = w1;
+                    w1 = wn;
+                }
             }
         }
         // ---- elimination levels 1 .. L-1 (previous row's kept tail by shuffle) ----
@@ -243,21 +281,12 @@ struct CrBlock {
         }
     }
 
-    // Row r from this thread's halves into the swizzled buffer (DTCR: float2 pairs (2m, 2m+1),
-    // even m written by parity 0, odd m by parity 1, exchanging values with the partner lane).
+    // Row r from this thread's halves into the swizzled buffer (DTCR: each lane stores its own
+    // parity's samples).
     __device__ __forceinline__ static void write_row(float* buf, const float (&u)[NPAR][M], int r, int p0) {
         if (SPLIT) {
 #pragma unroll(UNROLL ? 64 : 1)
-            for (int m = 0; m < M; m += 2) {
-                const float a = u[0][m], b = u[0][m + 1];
-                const float oa = __shfl_xor_sync(FULL_MASK, a, 1);
-                const float ob = __shfl_xor_sync(FULL_MASK, b, 1);
-                // parity 0 holds even samples: pair for m is (a, oa); parity 1's for m+1 is (ob, b)
-                if (p0 == 0)
-                    *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m)) = make_float2(a, oa);
-                else
-                    *reinterpret_cast<float2*>(buf + swz<N>(r, 2 * m + 2)) = make_float2(ob, b);
-            }
+            for (int m = 0; m < M; ++m) buf[swz<N>(r, 2 * m + p0)] = u[0][m];
         } else {
 #pragma unroll
             for (int j = 0; j < N / 4; ++j)
@@ -327,28 +356,21 @@ struct CrBlock {
 };
 
 
-// Single-section STCR / DTCR on the persistent pipeline (iir_pipe.cuh). P1 = the tile solve
-// of CrBlock (zero-state rows written back to the stage), the per-tile zero-state incoming
-// pairs and the chunk aggregate; P2 = the correction by the response to the chunk's incoming
-// state. The same float operations as CrBlock::filter_block, so the output is bit-identical
-// to the one-block-per-chunk schedule.
+// Single-section STCR / DTCR on the two-pass pipeline (iir_twopass.cuh): pass B is CrBlock's
+// section solve with the chunk's incoming state known from the start (tile solve, tile join,
+// response to the incoming state added in registers, one write of each row).
 template <bool SPLIT, int N_, int ROWS_, bool UNROLL>
-struct CrPipe {
+struct CrTwo {
     using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL>;
     static constexpr int N = N_, ROWS = ROWS_, M = Blk::M, NPAR = Blk::NPAR, RW = Blk::RW, NW = Blk::NW;
+    static constexpr int TPR = Blk::TPR;
 
-    __device__ __forceinline__ static void geometry(int w, int lane, int& rl, int& r, int& p0) {
-        rl = SPLIT ? (lane >> 1) : lane;
-        r = w * RW + rl;
-        p0 = SPLIT ? (lane & 1) : 0;
-    }
-
-    __device__ static void p1(const IirParams& p, float* buf, const float* hist, const float4* tc, float (*zin)[2],
-                              PipeAux* aux, int slot, uint32_t, int w, int lane) {
-        int rl, r, p0;
-        geometry(w, lane, rl, r, p0);
+    __device__ static void b_pass(const IirParams& p, float* buf, const float* hist, const float4* tc,
+                                  const float (*)[2], PipeAux* aux, float X0, float X1, int w, int lane) {
+        const int rl = SPLIT ? (lane >> 1) : lane;
+        const int r = w * RW + rl;
+        const int p0 = SPLIT ? (lane & 1) : 0;
         const IirSection& q = p.sec[0];
-        const float4 Ct = tc[RW - 1];  // C^RW
         float u[NPAR][M];
         float P0, P1;
         Blk::solve_tile(p, buf, q, 0, hist[30], hist[31], r, rl, p0, 0.f, 0.f, u, P0, P1);
@@ -357,60 +379,19 @@ struct CrPipe {
             aux->wtot[w][0][1] = P1;
         }
         named_barrier_rows(NW);  // every row read its input history; tile end pairs visible
-        Blk::write_row(buf, u, r, p0);
         float in0, in1;
-        warp_incoming(aux, w, 0, Ct, in0, in1);
-        if (lane == 0) {
-            zin[w][0] = in0;
-            zin[w][1] = in1;
-        }
-        if (w == NW - 1 && lane == 31) {
-            // chunk aggregate = C^RW (incoming of the last tile) + its end pair
-            float n0, n1;
-            mv2(Ct, in0, in1, n0, n1);
-            aux->partv[slot][0] = n0 + P0;
-            aux->partv[slot][1] = n1 + P1;
-        }
-    }
-
-    __device__ static void p2(const IirParams& p, float* buf, const float4* tc, const float (*zin)[2], float X0,
-                              float X1, uint32_t, int w, int lane) {
-        int rl, r, p0;
-        geometry(w, lane, rl, r, p0);
-        const IirSection& q = p.sec[0];
+        warp_incoming(aux, w, 0, tc[RW - 1], in0, in1);  // C^RW across a tile
         float S0 = X0, S1 = X1;
         if (w > 0) {
             float t0, t1;
             mv2(tc[RW * w - 1], X0, X1, t0, t1);  // C^(RW w)
-            S0 = t0 + zin[w][0];
-            S1 = t1 + zin[w][1];
+            S0 = t0 + in0;
+            S1 = t1 + in1;
         }
         float d2 = S0, d1 = S1;
         if (rl > 0) mv2(tc[rl - 1], S0, S1, d2, d1);  // C^rl
-        // In place on the row: STCR runs the response over the whole row; DTCR's two lanes
-        // take the row's two contiguous halves (A^(N/2) moves the incoming pair to the middle).
-        constexpr int SPAN = SPLIT ? N / 2 : N;
-        if (SPLIT && p0) {
-            float h2, h1;
-            mv2(tc[PipeGeom<ROWS, N, 2>::TC_HALF], d2, d1, h2, h1);
-            d2 = h2;
-            d1 = h1;
-        }
-        const int n0 = SPLIT ? p0 * (N / 2) : 0;
-#pragma unroll 4
-        for (int j = 0; j < SPAN / 4; ++j) {
-            float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, n0 + 4 * j));
-            const float4 v = *ptr;
-            float o[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float dn = fmaf(q.a1, d1, q.a2 * d2);
-                d2 = d1;
-                d1 = dn;
-                o[k] += dn;
-            }
-            *ptr = make_float4(o[0], o[1], o[2], o[3]);
-        }
+        Blk::add_response(u, q, p0, d2, d1);
+        Blk::write_row(buf, u, r, p0);
     }
 };
 

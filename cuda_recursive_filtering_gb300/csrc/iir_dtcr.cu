@@ -25,42 +25,42 @@ static void add(std::vector<KernelEntry>& reg) {
                                   0, ROWS});
 }
 
-template <int N, int ROWS, bool UNROLL, int S, int LAG>
-__global__ void __launch_bounds__(64 + CrPipe<true, N, ROWS, UNROLL>::NW * 32,
-                                  PipeGeom<ROWS, N, S>::min_blocks(64 + CrPipe<true, N, ROWS, UNROLL>::NW * 32))
-    iir_dtcr_pipe_kernel(const __grid_constant__ IirParams p) {
+template <int N, int ROWS, bool UNROLL, int S, int D>
+__global__ void __launch_bounds__(64 + CrTwo<true, N, ROWS, UNROLL>::NW * 32,
+                                  TwoPassGeom<ROWS, N, S, D>::min_blocks(64 + CrTwo<true, N, ROWS, UNROLL>::NW * 32))
+    iir_dtcr_two_kernel(const __grid_constant__ IirParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
-    run_pipeline<CrPipe<true, N, ROWS, UNROLL>, S, LAG>(p, smem);
+    run_twopass<CrTwo<true, N, ROWS, UNROLL>, S, D>(p, smem);
 }
 
-// Single-section persistent pipeline (chosen for one section when registered for the geometry).
-template <int N, int ROWS, bool UNROLL, int S, int LAG>
-static void add_pipe(std::vector<KernelEntry>& reg) {
-    using R = CrPipe<true, N, ROWS, UNROLL>;
+#ifndef IIR_TWO_STAGES
+#define IIR_TWO_STAGES 3
+#endif
+#ifndef IIR_TWO_LAG
+#define IIR_TWO_LAG 2
+#endif
+
+// Single-section two-pass kernel (chosen for one section when registered for the geometry).
+template <int N, int ROWS, bool UNROLL>
+static void add_two(std::vector<KernelEntry>& reg) {
+    using R = CrTwo<true, N, ROWS, UNROLL>;
     const int kind = UNROLL ? IIR_KIND_DTCR_UNROLL : IIR_KIND_DTCR;
     for (int b : {32, 64}) {
-        KernelEntry e{kind, b, N, (const void*)iir_dtcr_pipe_kernel<N, ROWS, UNROLL, S, LAG>,
-                      64 + R::NW * 32, PipeGeom<ROWS, N, S>::SMEM_BYTES, 0, ROWS};
+        KernelEntry e{kind, b, N, (const void*)iir_dtcr_two_kernel<N, ROWS, UNROLL, IIR_TWO_STAGES, IIR_TWO_LAG>,
+                      64 + R::NW * 32, TwoPassGeom<ROWS, N, IIR_TWO_STAGES, IIR_TWO_LAG>::SMEM_BYTES, 0, ROWS};
         e.pipeline = 1;
         reg.push_back(e);
     }
 }
 
-#ifndef IIR_DTCR_PIPE_STAGES
-#define IIR_DTCR_PIPE_STAGES 3
-#endif
-#ifndef IIR_DTCR_PIPE_LAG
-#define IIR_DTCR_PIPE_LAG 1
-#endif
-
 void register_dtcr(std::vector<KernelEntry>& reg) {
-    // (chunks of 8192 samples: 256 x 32, 128 x 64, 64 x 128)
-    add_pipe<32, 256, true, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
-    add_pipe<32, 256, false, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
-    add_pipe<64, 128, true, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
-    add_pipe<64, 128, false, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
-    add_pipe<128, 64, true, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
-    add_pipe<128, 64, false, IIR_DTCR_PIPE_STAGES, IIR_DTCR_PIPE_LAG>(reg);
+    // rows per chunk for 32, 64 and 128 samples per row: iir_pipe.cuh
+    add_two<32, IIR_PIPE_ROWS_N32, true>(reg);
+    add_two<32, IIR_PIPE_ROWS_N32, false>(reg);
+    add_two<64, IIR_PIPE_ROWS_N64, true>(reg);
+    add_two<64, IIR_PIPE_ROWS_N64, false>(reg);
+    add_two<128, IIR_PIPE_ROWS_N128, true>(reg);
+    add_two<128, IIR_PIPE_ROWS_N128, false>(reg);
     add<16, 64, false>(reg);
     add<32, 64, false>(reg);
     add<64, 64, false>(reg);

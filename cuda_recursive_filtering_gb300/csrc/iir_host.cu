@@ -297,7 +297,6 @@ struct iir_plan {
     size_t carry_cap = 0;      // chunks
     float4* d_tables = nullptr;
     float* d_fac = nullptr;    // PLR factor arrays
-    float4* d_qpow = nullptr;  // persistent pipeline: chunk transition powers Q^t, t < grid_max
     IirParams params{};
     IirPlrParams plr{};
     long long timeout_ns = 1000000000ll;
@@ -379,7 +378,6 @@ void plan_free(iir_plan* p) {
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_fac) cudaFree(p->d_fac);
-    if (p->d_qpow) cudaFree(p->d_qpow);
     delete p;
 }
 
@@ -560,21 +558,6 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     if (!st) st = cuda_status(cudaMalloc(&p->d_tables, tabs.size() * sizeof(float4)));
     if (!st)
         st = cuda_status(cudaMemcpy(p->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
-    if (!st && e->pipeline) {
-        // Q^t (FP64, rounded once) for the windowed lookback of the persistent pipeline
-        const M2 A{0.0, 1.0, static_cast<double>(secs[0].a2), static_cast<double>(secs[0].a1)};
-        const M2 Q = mpow(mpow(A, static_cast<unsigned long long>(N)), static_cast<unsigned long long>(e->rows));
-        std::vector<float4> qp(static_cast<size_t>(p->grid_max));
-        M2 P{1, 0, 0, 1};
-        for (int t = 0; t < p->grid_max; ++t) {
-            qp[t] = to_f4(P);
-            P = mmul(P, Q);
-        }
-        st = cuda_status(cudaMalloc(&p->d_qpow, qp.size() * sizeof(float4)));
-        if (!st) st = cuda_status(cudaMemcpy(p->d_qpow, qp.data(), qp.size() * sizeof(float4), cudaMemcpyHostToDevice));
-        q.qpow = p->d_qpow;
-        q.qpow_len = static_cast<unsigned int>(p->grid_max);
-    }
     if (st) {
         plan_free(p);
         return st;

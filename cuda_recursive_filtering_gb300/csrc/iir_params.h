@@ -77,9 +77,6 @@ struct IirParams {
     float gain;
     int pad0;
     unsigned long long* prof;         // per-block phase timestamps (IIR_PROFILE builds only)
-    const float4* qpow;               // persistent pipeline: Q^t, t < qpow_len (chunk transition powers)
-    unsigned int qpow_len;
-    int pad1;
     IirSection sec[IIR_MAX_SECTIONS];
 };
 

@@ -19,7 +19,7 @@
 // their loads and lookback waits overlap each other's filtering (the lookback latency is
 // set by the slowest predecessor's load, so concurrency, not a faster poll, hides it).
 #include "iir_device.cuh"
-#include "iir_pipe.cuh"
+#include "iir_twopass.cuh"
 #include "iir_registry.h"
 
 namespace iirgb {
@@ -198,18 +198,16 @@ struct PhBlock {
     }
 };
 
-// Single-section PH on the persistent pipeline (iir_pipe.cuh): P1 = the zero-state filter
-// pass + row-tail scan of filter_block, P2 = the correction pass with the chunk's incoming
-// state. The same float operations in the same order as filter_block, so both schedules
-// give bit-identical output.
+// Single-section PH on the two-pass pipeline (iir_twopass.cuh): pass B runs the true
+// recurrence over each row from its true incoming pair (pass A's zero-state incoming pair +
+// C^r X), one pass over the row.
 template <int N_, int ROWS_>
-struct PhPipe {
-    static constexpr int N = N_, ROWS = ROWS_, NW = ROWS / 32;
+struct PhTwo {
+    static constexpr int N = N_, ROWS = ROWS_, NW = ROWS / 32, TPR = 1;
     static_assert(ROWS % 32 == 0 && NW <= 16, "rows per block");
 
-    __device__ static void p1(const IirParams& p, float* buf, const float* hist, const float4* tc, float (*zin)[2],
-                              PipeAux* aux, int slot, uint32_t, int w, int lane) {
-        using Geo = PipeGeom<ROWS, N, 2>;
+    __device__ static void b_pass(const IirParams& p, float* buf, const float* hist, const float4* tc,
+                                  const float (*zin)[2], PipeAux*, float X0, float X1, int w, int lane) {
         const int r = w * 32 + lane;
         const IirSection& q = p.sec[0];
         const float gain = p.gain;
@@ -223,8 +221,14 @@ struct PhPipe {
         }
         xh2 *= gain;
         xh1 *= gain;
+        float y2 = X0, y1 = X1;  // true incoming pair (y[-2], y[-1]) of the row
+        if (r > 0) {
+            float q0, q1;
+            mv2(tc[r - 1], X0, X1, q0, q1);  // C^r X
+            y2 = zin[r][0] + q0;
+            y1 = zin[r][1] + q1;
+        }
         named_barrier_rows(NW);  // every row has its input history before rows are overwritten
-        float y1 = 0.f, y2 = 0.f;
 #pragma unroll 4
         for (int j = 0; j < N / 4; ++j) {
             float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
@@ -243,56 +247,14 @@ struct PhPipe {
             }
             *ptr = make_float4(ys[0], ys[1], ys[2], ys[3]);
         }
-        float s0 = y2, s1 = y1;
-        warp_scan2<32, 1>(s0, s1, q.M, lane);
-        if (lane == 31) {
-            aux->wtot[w][0][0] = s0;
-            aux->wtot[w][0][1] = s1;
-        }
-        named_barrier_rows(NW);
-        float in0 = 0.f, in1 = 0.f;
-        if (w > 0) {
-            warp_incoming(aux, w, 0, tc[Geo::TC_GPOW + 31], in0, in1);
-            float e0, e1;
-            mv2(tc[Geo::TC_GPOW + lane], in0, in1, e0, e1);
-            s0 += e0;
-            s1 += e1;
-        }
-        // zero-state incoming pair of row r = zero-state tail of row r - 1
-        float i0 = __shfl_up_sync(FULL_MASK, s0, 1);
-        float i1 = __shfl_up_sync(FULL_MASK, s1, 1);
-        if (lane == 0) {
-            i0 = in0;
-            i1 = in1;
-        }
-        zin[r][0] = i0;
-        zin[r][1] = i1;
-        if (r == ROWS - 1) {
-            aux->partv[slot][0] = s0;
-            aux->partv[slot][1] = s1;
-        }
-    }
-
-    __device__ static void p2(const IirParams& p, float* buf, const float4* tc, const float (*zin)[2], float X0,
-                              float X1, uint32_t, int w, int lane) {
-        const int r = w * 32 + lane;
-        const IirSection& q = p.sec[0];
-        float d2 = X0, d1 = X1;  // true incoming pair of the row
-        if (r > 0) {
-            float q0, q1;
-            mv2(tc[r - 1], X0, X1, q0, q1);  // C^r
-            d2 = zin[r][0] + q0;
-            d1 = zin[r][1] + q1;
-        }
-        PhBlock<32, N, ROWS>::correct_pass(buf, r, q.a1, q.a2, d2, d1);
     }
 };
 
-template <int N, int ROWS, int S, int LAG>
-__global__ void __launch_bounds__(64 + ROWS, PipeGeom<ROWS, N, S>::min_blocks(64 + ROWS))
-    iir_ph_pipe_kernel(const __grid_constant__ IirParams p) {
+template <int N, int ROWS, int S, int D>
+__global__ void __launch_bounds__(64 + ROWS, TwoPassGeom<ROWS, N, S, D>::min_blocks(64 + ROWS))
+    iir_ph_two_kernel(const __grid_constant__ IirParams p) {
     extern __shared__ __align__(128) unsigned char smem[];
-    run_pipeline<PhPipe<N, ROWS>, S, LAG>(p, smem);
+    run_twopass<PhTwo<N, ROWS>, S, D>(p, smem);
 }
 
 template <int B, int N, int ROWS>
@@ -308,30 +270,31 @@ static void add_ph(std::vector<KernelEntry>& reg) {
                               BlockGeom<ROWS, N>::SMEM_BYTES, 0, ROWS});
 }
 
-template <int B, int N, int ROWS, int S, int LAG>
-static void add_ph_pipe(std::vector<KernelEntry>& reg) {
-    KernelEntry e{IIR_KIND_PH, B, N, (const void*)iir_ph_pipe_kernel<N, ROWS, S, LAG>, 64 + ROWS,
-                  PipeGeom<ROWS, N, S>::SMEM_BYTES, 0, ROWS};
+#ifndef IIR_TWO_STAGES
+#define IIR_TWO_STAGES 3
+#endif
+#ifndef IIR_TWO_LAG
+#define IIR_TWO_LAG 2
+#endif
+
+// Single-section two-pass kernel (chosen for one section when registered for the geometry).
+template <int B, int N, int ROWS>
+static void add_ph_two(std::vector<KernelEntry>& reg) {
+    KernelEntry e{IIR_KIND_PH, B, N, (const void*)iir_ph_two_kernel<N, ROWS, IIR_TWO_STAGES, IIR_TWO_LAG>, 64 + ROWS,
+                  TwoPassGeom<ROWS, N, IIR_TWO_STAGES, IIR_TWO_LAG>::SMEM_BYTES, 0, ROWS};
     e.pipeline = 1;
     reg.push_back(e);
 }
 
-#ifndef IIR_PH_PIPE_STAGES
-#define IIR_PH_PIPE_STAGES 3
-#endif
-#ifndef IIR_PH_PIPE_LAG
-#define IIR_PH_PIPE_LAG 1
-#endif
-
 void register_ph(std::vector<KernelEntry>& reg) {
     // single-section pipeline (chosen for one section when registered for the geometry)
-    // (chunks of 8192 samples: 256 x 32, 128 x 64, 64 x 128)
-    add_ph_pipe<32, 32, 256, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
-    add_ph_pipe<64, 32, 256, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
-    add_ph_pipe<32, 64, 128, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
-    add_ph_pipe<64, 64, 128, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
-    add_ph_pipe<32, 128, 64, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
-    add_ph_pipe<64, 128, 64, IIR_PH_PIPE_STAGES, IIR_PH_PIPE_LAG>(reg);
+    // (rows per chunk for 32, 64 and 128 samples per row: iir_pipe.cuh)
+    add_ph_two<32, 32, IIR_PIPE_ROWS_N32>(reg);
+    add_ph_two<64, 32, IIR_PIPE_ROWS_N32>(reg);
+    add_ph_two<32, 64, IIR_PIPE_ROWS_N64>(reg);
+    add_ph_two<64, 64, IIR_PIPE_ROWS_N64>(reg);
+    add_ph_two<32, 128, IIR_PIPE_ROWS_N128>(reg);
+    add_ph_two<64, 128, IIR_PIPE_ROWS_N128>(reg);
     add_ph<32, 16, 128>(reg);
     add_ph<32, 32, 128>(reg);
     add_ph<32, 64, 128>(reg);

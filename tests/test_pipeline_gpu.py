@@ -1,8 +1,9 @@
-"""Single-section filters on the persistent pipeline (cooperative grid, TMA warp + lookback
-warp + row warps over shared-memory stages) against the FP64 oracle; run to run bit-identical
-(the windowed lookback adds its terms in a fixed order); and equal, within 1e-6 * max|ref|, to
-the one-block-per-chunk schedule of the same realization (IIR_GB300_SCHEDULE=ticket, run in a
-child process because the schedule is chosen once per process).
+"""Single-section filters on the persistent two-pass schedule (cooperative grid; TMA warp,
+lookback warp and row warps over shared-memory stages; every chunk read twice, the second time
+from L2) against the FP64 oracle, and equal within 1e-6 * max|ref| to the one-block-per-chunk
+schedule of the same realization (IIR_GB300_SCHEDULE=ticket, run in a child process because the
+schedule is chosen once per process) and to a second run of itself (the decoupled lookback may
+compose a carry from different predecessors in different launches, so runs agree to rounding).
 Tolerance: max|err| <= 1e-4 * max|ref| (src/test_accuracy.cu:178-188) and
 max|err| / RMS(ref) <= 1e-5 at order 2.
 """
@@ -103,6 +104,6 @@ def test_pipeline_deterministic_and_matches_ticket_schedule(tmp_path, cuda_devic
         y1 = p(xt).cpu().numpy()
         y2 = p(xt).cpu().numpy()
         p.check()
-        assert np.array_equal(y1, y2), k
         scale = float(np.max(np.abs(ref[k])))
+        assert np.max(np.abs(y1 - y2)) <= 1e-6 * scale, k
         assert np.max(np.abs(y1 - ref[k])) <= 1e-6 * scale, k
