@@ -7,7 +7,7 @@ launch-versioned decoupled lookback. The compute path is libiir_gb300.so (C ABI 
 include/iir_gb300.h); this package is its Python host mirror.
 """
 from ._lib import KERNELS, IirError, load as load_library
-from .api import Plan, PlrPlan, sosfilt
+from .api import Batch, Plan, PlrPlan, sosfilt
 
-__all__ = ["Plan", "PlrPlan", "sosfilt", "KERNELS", "IirError", "load_library"]
+__all__ = ["Plan", "PlrPlan", "Batch", "sosfilt", "KERNELS", "IirError", "load_library"]
 __version__ = "1.0.0"

@@ -26,6 +26,12 @@ KERNELS = {"AUTO": 0, "PH": 1, "STCR": 2, "STCR_UNROLL": 3, "DTCR": 4, "DTCR_UNR
 KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
 
 
+class IirSegment(ctypes.Structure):
+    """iir_segment (include/iir_gb300.h)."""
+    _fields_ = [("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("n", ctypes.c_size_t), ("filter", ctypes.c_int),
+                ("zi", ctypes.c_void_p), ("zf", ctypes.c_void_p)]
+
+
 class IirError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -68,6 +74,13 @@ def load(path: str | None = None):
         "iir_status_string": ([i], ctypes.c_char_p),
         "iir_version": ([], i),
         "iir_cache_clear": ([], i),
+        "iir_batch_create": ([pp, fp, ip, i, sz, sz], i),
+        "iir_batch_execute": ([vp, ctypes.POINTER(IirSegment), i, vp], i),
+        "iir_batch_check": ([vp, vp], i),
+        "iir_batch_set_timeout_ns": ([vp, ll], i),
+        "iir_batch_debug_withhold": ([vp, ll], i),
+        "iir_batch_filter_sections": ([vp, i], i),
+        "iir_batch_destroy": ([vp], i),
     }
     for name, (args, res) in sigs.items():
         f = getattr(L, name)

@@ -18,7 +18,7 @@ import torch
 from . import _lib
 from ._lib import KERNELS, KERNEL_NAMES, IirError, check
 
-__all__ = ["Plan", "PlrPlan", "sosfilt", "KERNELS", "IirError"]
+__all__ = ["Plan", "PlrPlan", "Batch", "sosfilt", "KERNELS", "IirError"]
 
 
 def _kernel_id(kernel) -> int:
@@ -168,3 +168,74 @@ def sosfilt(sos, x: torch.Tensor, kernel="AUTO", block_size: int = 0, n_blocks: 
                                  int(block_size), int(n_blocks), _stream_handle(stream))
     check(st, "iir_sos_filter")
     return out
+
+
+class Batch:
+    """Many independent signals in one launch (C ABI: iir_batch_*), each with its own filter.
+
+    ``filters`` is a list of SOS arrays (scipy rows), one per distinct filter. A call takes a
+    list of segments ``(x, y, filter_index, zi, zf)``: CUDA float32 tensors for input and
+    output, the filter's index, and optional device state in / out tensors of
+    ``state_size(filter)`` floats (None = start at rest / do not report). Segments are filtered
+    independently (PH solve; chunks of 4096 samples; the lookback stays inside a segment).
+    State layout: x[-2], x[-1] of the raw input, then each section's y[-2], y[-1].
+    """
+
+    def __init__(self, filters, max_segments: int = 1024, max_chunks: int = 1 << 16, device=None):
+        self._lib = _lib.load()
+        soss = [_sos_array(f) for f in filters]
+        if not soss:
+            raise ValueError("at least one filter")
+        self.n_sections = [int(s.shape[0]) for s in soss]
+        flat = np.ascontiguousarray(np.concatenate(soss, axis=0), np.float32)
+        ns = (ctypes.c_int * len(soss))(*self.n_sections)
+        self._ptr = ctypes.c_void_p()
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.device = dev
+        with torch.cuda.device(dev):
+            st = self._lib.iir_batch_create(ctypes.byref(self._ptr), flat.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                            ns, len(soss), int(max_segments), int(max_chunks))
+        check(st, "iir_batch_create")
+
+    def state_size(self, filter_index: int) -> int:
+        return 2 + 2 * self.n_sections[filter_index]
+
+    def __call__(self, segments, stream=None) -> None:
+        arr = (_lib.IirSegment * max(1, len(segments)))()
+        for i, seg in enumerate(segments):
+            x, y, f = seg[0], seg[1], int(seg[2])
+            zi = seg[3] if len(seg) > 3 else None
+            zf = seg[4] if len(seg) > 4 else None
+            _check_tensor(x, "x")
+            _check_tensor(y, "y")
+            if y.numel() != x.numel():
+                raise ValueError("y must have as many samples as x")
+            for z, name in ((zi, "zi"), (zf, "zf")):
+                if z is not None:
+                    _check_tensor(z, name)
+                    if z.numel() != self.state_size(f):
+                        raise ValueError(f"{name} must hold {self.state_size(f)} floats")
+            arr[i] = _lib.IirSegment(x.data_ptr(), y.data_ptr(), x.numel(), f,
+                                     zi.data_ptr() if zi is not None else None,
+                                     zf.data_ptr() if zf is not None else None)
+        check(self._lib.iir_batch_execute(self._ptr, arr, len(segments), _stream_handle(stream)), "iir_batch_execute")
+
+    def check(self, stream=None) -> None:
+        check(self._lib.iir_batch_check(self._ptr, _stream_handle(stream)), "device")
+
+    def set_timeout_ns(self, ns: int) -> None:
+        check(self._lib.iir_batch_set_timeout_ns(self._ptr, int(ns)))
+
+    def debug_withhold(self, chunk: int) -> None:
+        check(self._lib.iir_batch_debug_withhold(self._ptr, int(chunk)))
+
+    def close(self) -> None:
+        if getattr(self, "_ptr", None) is not None and self._ptr.value:
+            self._lib.iir_batch_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,546 @@
+// iir_batch.cu — batched segments: many independent signals in one launch.
+//
+// A segment is one signal (a channel, or the next chunk of a live stream) with its own
+// cascade (any number of sections up to IIR_MAX_SECTIONS), an optional state in (zi) and an
+// optional state out (zf). The launch's chunks are the concatenation of every segment's
+// chunks; blocks take them in ticket order (one block per chunk, as iir_ph_kernel), find
+// their segment by binary search, and run the PH section solve (iir_ph.cuh) with the
+// decoupled lookback restricted to the segment: a segment's first chunk starts from zi, and
+// the lookback treats zi as the state before the segment. The block that holds a segment's
+// last sample writes zf. The reference filters one signal with one compile-time filter per
+// launch (ph_kernels.cuh:151-200, src/test_accuracy.cu:146); this is the batching form that
+// design cannot express.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/iir_gb300.h"
+#include "iir_host_internal.h"
+#include "iir_ph.cuh"
+#include "iir_registry.h"
+
+namespace iirgb {
+
+struct BatchAux {
+    unsigned int chunk, epoch, seg;
+    int bail;
+    float wtot[16][2][2];
+    float X[2];
+};
+
+struct BatchBlock {
+    static constexpr int N = IIR_BATCH_N, ROWS = IIR_BATCH_ROWS, NW = ROWS / 32, THREADS = 32 + ROWS;
+    static constexpr int CHUNK = ROWS * N;
+    using Ph = PhBlock<32, N, ROWS>;
+    static constexpr size_t SMEM_BYTES = CHUNK * sizeof(float) + sizeof(BatchAux) + 16;
+
+    // Incoming state of the segment's chunk lc for section `sec` (lookback within the segment).
+    __device__ static bool control(const IirBatchParams& p, BatchAux* aux, const IirBatchSegment& sg, int sec,
+                                   uint32_t lc, uint32_t epoch, const float4* tab, float4 Gw) {
+        const int lane = threadIdx.x & 31;
+        float t0 = 0.f, t1 = 0.f;
+#pragma unroll 4
+        for (int w = 0; w < NW; ++w) {
+            float n0, n1;
+            mv2(Gw, t0, t1, n0, n1);
+            t0 = n0 + aux->wtot[w][0][0];
+            t1 = n1 + aux->wtot[w][0][1];
+        }
+        const float z0 = sg.zi ? sg.zi[2 + 2 * sec] : 0.f;
+        const float z1 = sg.zi ? sg.zi[3 + 2 * sec] : 0.f;
+        unsigned long long* level = p.carry + static_cast<size_t>(sec) * p.carry_stride;
+        unsigned long long* slots = level + static_cast<size_t>(sg.chunk0) * 4;
+        unsigned long long* gslots = level + static_cast<size_t>(p.carry_cap) * 4 + static_cast<size_t>(sg.group0) * 4;
+        const bool withhold = static_cast<long long>(sg.chunk0 + lc) == p.withhold_chunk;
+        const uint32_t pf = 2u * epoch + 1u, ff = 2u * epoch + 2u;
+        if (lane == 0 && !withhold) publish2(slots + static_cast<size_t>(lc) * 4, pf, t0, t1);
+        float X0 = z0, X1 = z1;
+        bool ok = true;
+        if (lc > 0)
+            ok = lookback_hier(p, slots, gslots, tab + IIR_BT_QC, tab + IIR_BT_QG, lc, epoch, t0, t1, withhold, X0, X1,
+                               z0, z1);
+        if (lane == 0) {
+            if (ok && !withhold) {
+                float f0, f1;
+                mv2(tab[IIR_BT_QC + 1], X0, X1, f0, f1);
+                publish2(slots + static_cast<size_t>(lc) * 4 + 2, ff, t0 + f0, t1 + f1);
+                if ((lc & 31u) == 31u) publish2(gslots + static_cast<size_t>(lc >> 5) * 4 + 2, ff, t0 + f0, t1 + f1);
+            }
+            aux->X[0] = X0;
+            aux->X[1] = X1;
+            aux->bail = ok ? 0 : 1;
+        }
+        return ok;
+    }
+
+    __device__ static void run(const IirBatchParams& p, unsigned char* smem) {
+        float* buf = reinterpret_cast<float*>(smem);
+        BatchAux* aux = reinterpret_cast<BatchAux*>(smem + CHUNK * sizeof(float));
+        const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+        if (warp == 0) {
+            uint32_t epoch = 0, c = 0;
+            if (lane == 0) c = take_ticket(p.state, p.nchunks, epoch);
+            c = __shfl_sync(FULL_MASK, c, 0);
+            epoch = __shfl_sync(FULL_MASK, epoch, 0);
+            // segment holding chunk c: the last s with chunk_start[s] <= c (empty segments share
+            // their start with the next one, so the last such index is the non-empty one).
+            // 32-way search: each round the lanes probe 32 evenly spaced starts of [lo, hi).
+            uint32_t lo = 0, hi = p.nsegs;  // answer in [lo, hi)
+            while (hi - lo > 1) {
+                const uint32_t span = hi - lo;
+                const uint32_t probe = lo + static_cast<uint32_t>((static_cast<unsigned long long>(span) * lane) / 32);
+                const bool le = p.chunk_start[probe] <= c;
+                const unsigned m = __ballot_sync(FULL_MASK, le);  // lanes 0..k-1 hold (starts ascend)
+                const int k = 32 - __clz(m);                        // highest lane with start <= c, + 1
+                const uint32_t nlo = lo + static_cast<uint32_t>((static_cast<unsigned long long>(span) * (k - 1)) / 32);
+                const uint32_t nhi = (k < 32) ? lo + static_cast<uint32_t>((static_cast<unsigned long long>(span) * k) / 32)
+                                              : hi;
+                lo = nlo;
+                hi = nhi > nlo ? nhi : nlo + 1;
+            }
+            if (lane == 0) {
+                aux->chunk = c;
+                aux->epoch = epoch;
+                aux->seg = lo;
+                aux->bail = 0;
+            }
+        }
+        __syncthreads();
+        const uint32_t c = aux->chunk, epoch = aux->epoch;
+        const IirBatchSegment sg = p.segs[aux->seg];
+        const IirBatchFilter flt = p.filters[sg.filter];
+        const uint32_t lc = c - sg.chunk0;
+        const long long cs = static_cast<long long>(lc) * CHUNK;
+        const long long nrem = sg.n - cs;  // samples of the segment from this chunk's start (> 0)
+        if (nrem >= CHUNK && (reinterpret_cast<uintptr_t>(sg.x) & 15u) == 0) {
+            // whole chunk, 16-byte aligned: float4 loads, all issued before the stores
+            constexpr int V = CHUNK / 4, PER = (V + THREADS - 1) / THREADS;
+            const float4* src = reinterpret_cast<const float4*>(sg.x + cs);
+            float4 v[PER];
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int i = tid + k * THREADS;
+                if (i < V) v[k] = __ldg(src + i);
+            }
+#pragma unroll
+            for (int k = 0; k < PER; ++k) {
+                const int i = tid + k * THREADS;
+                if (i < V) *reinterpret_cast<float4*>(buf + swz<N>((4 * i) / N, (4 * i) % N)) = v[k];
+            }
+        } else {
+            for (int i = tid; i < CHUNK; i += THREADS) buf[swz<N>(i / N, i % N)] = (i < nrem) ? sg.x[cs + i] : 0.f;
+        }
+        __syncthreads();
+
+        const bool row_warp = warp > 0;
+        const int w = warp - 1;
+        const int r = w * 32 + lane;
+        const float gain = flt.gain;
+        float xh2 = 0.f, xh1 = 0.f;
+        if (row_warp) {
+            if (r > 0) {
+                xh2 = buf[swz<N>(r - 1, N - 2)];
+                xh1 = buf[swz<N>(r - 1, N - 1)];
+            } else if (lc > 0) {
+                xh2 = sg.x[cs - 2];
+                xh1 = sg.x[cs - 1];
+            } else if (sg.zi) {
+                xh2 = sg.zi[0];
+                xh1 = sg.zi[1];
+            }
+            xh2 *= gain;
+            xh1 *= gain;
+            named_barrier_rows(NW);
+            if (gain != 1.f) {
+#pragma unroll 4
+                for (int j = 0; j < N / 4; ++j) {
+                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+                    const float4 v = *ptr;
+                    *ptr = make_float4(v.x * gain, v.y * gain, v.z * gain, v.w * gain);
+                }
+            }
+        }
+        // positions of the segment's last two samples relative to this chunk
+        const long long m1 = nrem - 1, m2 = nrem - 2;  // in [0, CHUNK) when inside this chunk
+        float pa1 = 0.f, pa2 = 0.f, d2 = 0.f, d1 = 0.f;
+        for (int sec = 0; sec < flt.n_sections; ++sec) {
+            const IirSection& q = p.secs[flt.sec0 + sec];
+            const float4* tab = p.tables + static_cast<size_t>(flt.sec0 + sec) * IIR_BT_STRIDE;
+            const float4 Gw = tab[IIR_BT_GPOW + 31];
+            float s0 = 0.f, s1 = 0.f, in0 = 0.f, in1 = 0.f;
+            if (row_warp) {
+                if (sec == 0)
+                    Ph::template filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1);
+                else
+                    Ph::template filter_pass<true>(buf, r, q.b1, q.b2, q.a1, q.a2, pa1, pa2, d2, d1, xh2, xh1, s0, s1);
+                warp_scan2<32, 1>(s0, s1, q.M, lane);
+                if (lane == 31) {
+                    aux->wtot[w][0][0] = s0;
+                    aux->wtot[w][0][1] = s1;
+                }
+            }
+            __syncthreads();  // (A)
+            if (row_warp) {
+                warp_incoming(aux, w, 0, Gw, in0, in1);
+                if (w > 0) {
+                    float e0, e1;
+                    mv2(tab[IIR_BT_GPOW + lane], in0, in1, e0, e1);
+                    s0 += e0;
+                    s1 += e1;
+                }
+            } else {
+                control(p, aux, sg, sec, lc, epoch, tab, Gw);
+            }
+            __syncthreads();  // (B)
+            if (aux->bail) return;
+            if (row_warp) {
+                const float X0 = aux->X[0], X1 = aux->X[1];
+                float P0, P1;
+                mv2(tab[IIR_BT_CPOW + r], X0, X1, P0, P1);
+                const float T0 = s0 + P0, T1 = s1 + P1;
+                float i0 = __shfl_up_sync(FULL_MASK, T0, 1);
+                float i1 = __shfl_up_sync(FULL_MASK, T1, 1);
+                if (lane == 0) {
+                    if (r == 0) {
+                        i0 = X0;
+                        i1 = X1;
+                    } else {
+                        float q0, q1;
+                        mv2(tab[IIR_BT_CPOW + r - 1], X0, X1, q0, q1);
+                        i0 = in0 + q0;
+                        i1 = in1 + q1;
+                    }
+                }
+                if (sg.zf) {
+                    // this section's true output at the segment's last two samples: the row's
+                    // zero-state value + the response to the row's incoming pair (i0, i1)
+                    const long long rs = static_cast<long long>(r) * N;
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        const long long m = t == 0 ? m2 : m1;
+                        if (m >= rs && m < rs + N) {
+                            float e2 = i0, e1 = i1, dn = 0.f;
+                            for (int k = 0; k <= static_cast<int>(m - rs); ++k) {
+                                dn = fmaf(q.a1, e1, q.a2 * e2);
+                                e2 = e1;
+                                e1 = dn;
+                            }
+                            sg.zf[2 + 2 * sec + t] = buf[swz<N>(r, static_cast<int>(m - rs))] + dn;
+                        }
+                    }
+                    // the second-to-last sample in the previous chunk: the chunk's incoming y[-1]
+                    if (r == 0 && lane == 0 && m2 == -1) sg.zf[2 + 2 * sec] = X1;
+                }
+                pa1 = q.a1;
+                pa2 = q.a2;
+                d2 = i0;
+                d1 = i1;
+                xh2 = i0;
+                xh1 = i1;
+            }
+        }
+        if (row_warp) Ph::correct_pass(buf, r, pa1, pa2, d2, d1);
+        __syncthreads();
+        const long long cnt = nrem < CHUNK ? nrem : CHUNK;
+        if (cnt == CHUNK && (reinterpret_cast<uintptr_t>(sg.y) & 15u) == 0) {
+            float4* dst = reinterpret_cast<float4*>(sg.y + cs);
+            for (int i = tid; i < CHUNK / 4; i += THREADS)
+                dst[i] = *reinterpret_cast<const float4*>(buf + swz<N>((4 * i) / N, (4 * i) % N));
+        } else {
+            for (int i = tid; i < cnt; i += THREADS) sg.y[cs + i] = buf[swz<N>(i / N, i % N)];
+        }
+        if (sg.zf && tid == 0 && nrem <= CHUNK) {
+            // input history after the segment (raw)
+            sg.zf[1] = sg.x[sg.n - 1];
+            sg.zf[0] = sg.n >= 2 ? sg.x[sg.n - 2] : (sg.zi ? sg.zi[1] : 0.f);
+        }
+    }
+};
+
+__global__ void __launch_bounds__(BatchBlock::THREADS, 6) iir_batch_kernel(const __grid_constant__ IirBatchParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    BatchBlock::run(p, smem);
+}
+
+}  // namespace iirgb
+
+// -------------------------------------------------------------------------------------------
+// host side
+// -------------------------------------------------------------------------------------------
+using namespace iirgb;
+using namespace iirhost;
+
+struct iir_batch {
+    int device = 0;
+    int n_filters = 0;
+    int max_sections = 0;
+    IirBatchFilter* d_filters = nullptr;
+    IirSection* d_secs = nullptr;
+    float4* d_tables = nullptr;
+    IirLaunchState* d_state = nullptr;
+    unsigned long long* d_carry = nullptr;
+    size_t carry_cap = 0, gcap = 0, carry_bytes = 0;
+    IirBatchSegment* d_segs = nullptr;
+    unsigned int* d_starts = nullptr;
+    size_t seg_cap = 0;
+    // pinned staging for the segment table, two buffers used in turn (an event guards reuse)
+    unsigned char* h_stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    int stage_turn = 0;
+    std::vector<int> filter_sections;
+    long long timeout_ns = 1000000000ll;
+    long long withhold = -1;
+    unsigned long long launches = 0;
+};
+
+namespace {
+
+size_t stage_bytes(size_t segs) { return segs * sizeof(IirBatchSegment) + (segs + 1) * sizeof(unsigned int) + 64; }
+
+void batch_free_segments(iir_batch* b) {
+    if (b->d_segs) cudaFree(b->d_segs);
+    if (b->d_starts) cudaFree(b->d_starts);
+    for (int i = 0; i < 2; ++i) {
+        if (b->h_stage[i]) cudaFreeHost(b->h_stage[i]);
+        b->h_stage[i] = nullptr;
+    }
+    b->d_segs = nullptr;
+    b->d_starts = nullptr;
+    b->seg_cap = 0;
+}
+
+int batch_alloc_segments(iir_batch* b, size_t segs) {
+    batch_free_segments(b);
+    segs = std::max<size_t>(segs, 16);
+    int st = cuda_status(cudaMalloc(&b->d_segs, segs * sizeof(IirBatchSegment)));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_starts, (segs + 1) * sizeof(unsigned int)));
+    for (int i = 0; i < 2 && !st; ++i) st = cuda_status(cudaMallocHost(&b->h_stage[i], stage_bytes(segs)));
+    if (st) return st;
+    b->seg_cap = segs;
+    return IIR_OK;
+}
+
+int batch_alloc_carry(iir_batch* b, size_t chunks, size_t segs) {
+    if (b->d_carry) cudaFree(b->d_carry);
+    b->d_carry = nullptr;
+    chunks = std::max<size_t>(chunks, 64);
+    const size_t gcap = chunks / IIR_GROUP + segs + 2;
+    const size_t words = 4 * (chunks + gcap);
+    const size_t bytes = words * sizeof(unsigned long long) * static_cast<size_t>(b->max_sections);
+    int st = cuda_status(cudaMalloc(&b->d_carry, bytes));
+    if (!st) st = cuda_status(cudaMemset(b->d_carry, 0, bytes));
+    if (!st) st = cuda_status(cudaMemset(b->d_state, 0, sizeof(IirLaunchState)));
+    if (st) return st;
+    b->carry_cap = chunks;
+    b->gcap = gcap;
+    b->carry_bytes = bytes;
+    b->launches = 0;
+    return IIR_OK;
+}
+
+void batch_free(iir_batch* b) {
+    if (!b) return;
+    cudaDeviceSynchronize();
+    batch_free_segments(b);
+    for (int i = 0; i < 2; ++i)
+        if (b->stage_done[i]) cudaEventDestroy(b->stage_done[i]);
+    if (b->d_filters) cudaFree(b->d_filters);
+    if (b->d_secs) cudaFree(b->d_secs);
+    if (b->d_tables) cudaFree(b->d_tables);
+    if (b->d_state) cudaFree(b->d_state);
+    if (b->d_carry) cudaFree(b->d_carry);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, int n_filters, size_t max_segments,
+                     size_t max_chunks) {
+    if (!out || !sos || !n_sections || n_filters < 1) return IIR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::vector<IirBatchFilter> filters(static_cast<size_t>(n_filters));
+    std::vector<IirSection> secs;
+    std::vector<float4> tabs;
+    std::vector<float4> full(IIR_TAB_STRIDE);
+    int max_sec = 1;
+    size_t off = 0;
+    for (int f = 0; f < n_filters; ++f) {
+        const int ns = n_sections[f];
+        if (ns < 1 || ns > IIR_MAX_SECTIONS) return IIR_ERR_INVALID_ARGUMENT;
+        SectionF32 s32[IIR_MAX_SECTIONS];
+        double gain = 1.0;
+        int st = normalise_sos(sos + 6 * off, ns, s32, gain);
+        if (st) return st;
+        filters[f] = IirBatchFilter{static_cast<float>(gain), ns, static_cast<int>(secs.size()), 0};
+        for (int k = 0; k < ns; ++k) {
+            IirSection q;
+            st = precompute_section(s32[k], IIR_KIND_PH, IIR_BATCH_ROWS, IIR_BATCH_N, q, full.data());
+            if (st) return st;
+            secs.push_back(q);
+            const size_t base = tabs.size();
+            tabs.resize(base + IIR_BT_STRIDE, make_float4(0, 0, 0, 0));
+            for (int r = 0; r < IIR_BATCH_ROWS; ++r) tabs[base + IIR_BT_CPOW + r] = full[IIR_TAB_CPOW + r];
+            for (int t = 0; t < 32; ++t) tabs[base + IIR_BT_GPOW + t] = full[IIR_TAB_GPOW + t];
+            for (int l = 0; l <= 32; ++l) {
+                tabs[base + IIR_BT_QC + l] = full[IIR_TAB_QC + l];
+                tabs[base + IIR_BT_QG + l] = full[IIR_TAB_QG + l];
+            }
+        }
+        max_sec = std::max(max_sec, ns);
+        off += static_cast<size_t>(ns);
+    }
+    iir_batch* b = new iir_batch();
+    b->n_filters = n_filters;
+    b->max_sections = max_sec;
+    b->filter_sections.assign(n_sections, n_sections + n_filters);
+    int st = cuda_status(cudaGetDevice(&b->device));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_filters, filters.size() * sizeof(IirBatchFilter)));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_secs, secs.size() * sizeof(IirSection)));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4)));
+    if (!st)
+        st = cuda_status(cudaMemcpy(b->d_filters, filters.data(), filters.size() * sizeof(IirBatchFilter),
+                                    cudaMemcpyHostToDevice));
+    if (!st) st = cuda_status(cudaMemcpy(b->d_secs, secs.data(), secs.size() * sizeof(IirSection), cudaMemcpyHostToDevice));
+    if (!st)
+        st = cuda_status(cudaMemcpy(b->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_state, sizeof(IirLaunchState)));
+    if (!st) st = batch_alloc_segments(b, max_segments);
+    if (!st) st = batch_alloc_carry(b, max_chunks, b->seg_cap);
+    for (int i = 0; i < 2 && !st; ++i) st = cuda_status(cudaEventCreateWithFlags(&b->stage_done[i], cudaEventDisableTiming));
+    if (!st)
+        st = cuda_status(cudaFuncSetAttribute(reinterpret_cast<const void*>(iir_batch_kernel),
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              static_cast<int>(BatchBlock::SMEM_BYTES)));
+    if (st) {
+        batch_free(b);
+        return st;
+    }
+    *out = b;
+    return IIR_OK;
+}
+
+int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* stream_) {
+    if (!b || n_segs < 0 || (n_segs > 0 && !segs)) return IIR_ERR_INVALID_ARGUMENT;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    // validate and count chunks
+    size_t total = 0, groups = 0;
+    for (int i = 0; i < n_segs; ++i) {
+        const iir_segment& s = segs[i];
+        if (s.filter < 0 || s.filter >= b->n_filters) return IIR_ERR_INVALID_ARGUMENT;
+        if (s.n > 0 && (!s.x || !s.y)) return IIR_ERR_INVALID_ARGUMENT;
+        if (s.n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
+        const char* xb = reinterpret_cast<const char*>(s.x);
+        const char* yb = reinterpret_cast<const char*>(s.y);
+        if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
+        const size_t ch = (s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK;
+        total += ch;
+        groups += (ch + IIR_GROUP - 1) / IIR_GROUP;
+    }
+    if (total == 0) return IIR_OK;
+    if (total > 0x7fffffffull) return IIR_ERR_TOO_LARGE;
+    if (static_cast<size_t>(n_segs) > b->seg_cap) {
+        cudaStreamSynchronize(stream);
+        const int st = batch_alloc_segments(b, static_cast<size_t>(n_segs) * 2);
+        if (st) return st;
+    }
+    if (total > b->carry_cap || groups > b->gcap) {
+        cudaStreamSynchronize(stream);
+        const int st = batch_alloc_carry(b, std::max(total, b->carry_cap * 2), std::max<size_t>(n_segs, groups));
+        if (st) return st;
+    }
+    if (++b->launches >= (1ull << 30)) {
+        int st = cuda_status(cudaMemsetAsync(b->d_carry, 0, b->carry_bytes, stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, sizeof(IirLaunchState), stream));
+        if (st) return st;
+        b->launches = 1;
+    }
+    // segment table into a pinned staging buffer (wait until its previous copy has left)
+    const int turn = b->stage_turn;
+    b->stage_turn ^= 1;
+    int st = cuda_status(cudaEventSynchronize(b->stage_done[turn]));
+    if (st) return st;
+    IirBatchSegment* hs = reinterpret_cast<IirBatchSegment*>(b->h_stage[turn]);
+    unsigned int* hstart = reinterpret_cast<unsigned int*>(b->h_stage[turn] + n_segs * sizeof(IirBatchSegment));
+    unsigned int chunk0 = 0, group0 = 0;
+    for (int i = 0; i < n_segs; ++i) {
+        const iir_segment& s = segs[i];
+        const unsigned int ch = static_cast<unsigned int>((s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK);
+        hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, chunk0, group0, s.filter, 0};
+        hstart[i] = chunk0;
+        chunk0 += ch;
+        group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;
+    }
+    hstart[n_segs] = chunk0;
+    st = cuda_status(cudaMemcpyAsync(b->d_segs, hs, n_segs * sizeof(IirBatchSegment), cudaMemcpyHostToDevice, stream));
+    if (!st)
+        st = cuda_status(cudaMemcpyAsync(b->d_starts, hstart, (n_segs + 1) * sizeof(unsigned int),
+                                         cudaMemcpyHostToDevice, stream));
+    if (!st) st = cuda_status(cudaEventRecord(b->stage_done[turn], stream));
+    if (st) return st;
+    IirBatchParams q{};
+    q.segs = b->d_segs;
+    q.chunk_start = b->d_starts;
+    q.filters = b->d_filters;
+    q.secs = b->d_secs;
+    q.tables = b->d_tables;
+    q.carry = b->d_carry;
+    q.state = b->d_state;
+    q.carry_stride = 4 * (b->carry_cap + b->gcap);
+    q.timeout_ns = b->timeout_ns;
+    q.withhold_chunk = b->withhold;
+    q.nsegs = static_cast<unsigned int>(n_segs);
+    q.nchunks = static_cast<unsigned int>(total);
+    q.carry_cap = static_cast<unsigned int>(b->carry_cap);
+    q.max_sections = b->max_sections;
+    b->withhold = -1;
+    void* args[] = {&q};
+    return cuda_status(cudaLaunchKernel(reinterpret_cast<const void*>(iir_batch_kernel), dim3(static_cast<unsigned>(total)),
+                                        dim3(BatchBlock::THREADS), args, BatchBlock::SMEM_BYTES, stream));
+}
+
+int iir_batch_check(iir_batch* b, void* stream_) {
+    if (!b) return IIR_ERR_INVALID_ARGUMENT;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    int st = cuda_status(cudaStreamSynchronize(stream));
+    if (st) return st;
+    IirLaunchState hs;
+    st = cuda_status(cudaMemcpy(&hs, b->d_state, sizeof(hs), cudaMemcpyDeviceToHost));
+    if (st) return st;
+    if (hs.error == 0ull) return IIR_OK;
+    const unsigned long long zero = 0ull;
+    cudaMemcpy(reinterpret_cast<char*>(b->d_state) + offsetof(IirLaunchState, error), &zero, sizeof(zero),
+               cudaMemcpyHostToDevice);
+    const unsigned code = static_cast<unsigned>(hs.error & 0xffffffffull);
+    return code == IIR_DEV_ERR_TIMEOUT ? IIR_ERR_LOOKBACK_TIMEOUT : IIR_ERR_CUDA;
+}
+
+int iir_batch_set_timeout_ns(iir_batch* b, long long timeout_ns) {
+    if (!b || timeout_ns <= 0) return IIR_ERR_INVALID_ARGUMENT;
+    b->timeout_ns = timeout_ns;
+    return IIR_OK;
+}
+
+int iir_batch_debug_withhold(iir_batch* b, long long chunk) {
+    if (!b) return IIR_ERR_INVALID_ARGUMENT;
+    b->withhold = chunk;
+    return IIR_OK;
+}
+
+int iir_batch_filter_sections(const iir_batch* b, int filter) {
+    if (!b || filter < 0 || filter >= b->n_filters) return IIR_ERR_INVALID_ARGUMENT;
+    return b->filter_sections[static_cast<size_t>(filter)];
+}
+
+int iir_batch_destroy(iir_batch* b) {
+    if (!b) return IIR_ERR_INVALID_ARGUMENT;
+    batch_free(b);
+    return IIR_OK;
+}
+
+}  // extern "C"

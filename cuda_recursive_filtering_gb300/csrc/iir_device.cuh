@@ -238,11 +238,12 @@ __device__ __forceinline__ bool lookback_give_up(const P& p, uint32_t epoch, uin
 // The last chunk of a group (j = 31) publishes the group aggregate
 // gpart(g) = sum_{i<=31} Q^(31-i) part(i) as soon as its group's partials are visible; its
 // own inclusive carry is the group's (published by the caller).
-// Tables: Qc[l] = Q^l (l <= 32), Qg[l] = Q^(32 l) (l <= 32).
+// Tables: Qc[l] = Q^l (l <= 32), Qg[l] = Q^(32 l) (l <= 32). (z0, z1) is the state before
+// chunk 0 (the incoming state of a stream segment; zero for a signal that starts at rest).
 template <class P>
 __device__ bool lookback_hier(const P& p, const unsigned long long* slots, unsigned long long* gslots,
                               const float4* Qc, const float4* Qg, uint32_t c, uint32_t epoch, float own0, float own1,
-                              bool withhold, float& X0, float& X1) {
+                              bool withhold, float& X0, float& X1, float z0 = 0.f, float z1 = 0.f) {
     const int lane = threadIdx.x & 31;
     const uint32_t pf = 2u * epoch + 1u, ff = 2u * epoch + 2u;
     const int j = static_cast<int>(c & 31u);
@@ -266,8 +267,11 @@ __device__ bool lookback_hier(const P& p, const unsigned long long* slots, unsig
         if (gm >= 0) {
             gs = read_slot(gslots + static_cast<size_t>(gm) * 4, pf, ff);
         } else {
-            gs.part = gs.full = true;  // before the signal: zero state
-            gs.p0 = gs.p1 = gs.f0 = gs.f1 = 0.f;
+            // before the signal: the state at its start, (z0, z1) (zero unless given)
+            gs.part = gs.full = true;
+            gs.p0 = gs.p1 = 0.f;
+            gs.f0 = z0;
+            gs.f1 = z1;
         }
         IIR_PROF_ADD(p, 6, lane == 0 ? 1ull : 0ull);
         // group aggregate of a group's last chunk

@@ -101,5 +101,56 @@ struct IirPlrParams {
 };
 
 // Status codes stored in IirLaunchState::error (same values as the C ABI).
+// ------------------------------------------------------------------------------------------
+// Batched segments: many independent signals (channels / stream chunks) in one launch, each
+// with its own filter and optional state in / state out.
+// State layout (zi / zf, 2 + 2 * n_sections floats): x[-2], x[-1] (raw input), then per
+// section its output history y[-2], y[-1].
+// Compact lane tables per section (rows = IIR_BATCH_ROWS):
+#define IIR_BATCH_ROWS 128
+#define IIR_BATCH_N 32
+#define IIR_BT_CPOW 0      // C^(r+1), r < IIR_BATCH_ROWS
+#define IIR_BT_GPOW 128    // C^(t+1), t < 32
+#define IIR_BT_QC 160      // Q^l, l <= 32
+#define IIR_BT_QG 193      // Q^(32 l), l <= 32
+#define IIR_BT_STRIDE 228
+
+struct IirBatchFilter {
+    float gain;
+    int n_sections;
+    int sec0;               // index of its first section in the section / table arrays
+    int pad;
+};
+
+struct IirBatchSegment {
+    const float* x;
+    float* y;
+    long long n;
+    const float* zi;        // state in (device) or null = at rest
+    float* zf;              // state out (device) or null
+    unsigned int chunk0;    // first chunk of the segment in the launch's chunk space
+    unsigned int group0;    // first group slot of the segment
+    int filter;
+    int pad;
+};
+
+struct IirBatchParams {
+    const IirBatchSegment* segs;
+    const unsigned int* chunk_start;  // [nsegs + 1], chunk_start[i] = segs[i].chunk0
+    const IirBatchFilter* filters;
+    const IirSection* secs;
+    const float4* tables;             // [sections][IIR_BT_STRIDE]
+    unsigned long long* carry;        // per section level: [carry_cap][4] chunk slots, then [gcap][4] group slots
+    IirLaunchState* state;
+    unsigned long long carry_stride;  // words per section level
+    long long timeout_ns;
+    long long withhold_chunk;         // fault injection (-1 = off)
+    unsigned int nsegs;
+    unsigned int nchunks;
+    unsigned int carry_cap;
+    int max_sections;
+    unsigned long long* prof;         // unused (shared helpers' profiling hook)
+};
+
 #define IIR_DEV_ERR_TIMEOUT 4u
 #define IIR_DEV_ERR_MBARRIER 7u

@@ -133,6 +133,40 @@ int iir_plan_launches_per_execute(const iir_plan* plan);
 
 int iir_plan_destroy(iir_plan* plan);
 
+/* ---- batched segments (no reference counterpart: the reference filters one signal with
+ * one compile-time filter per launch, ph_kernels.cuh:151-200, src/test_accuracy.cu:146) ------ */
+
+/* One independent signal of a batch: a channel, or the next chunk of a live stream.
+ * zi / zf are device arrays of 2 + 2 * n_sections floats: x[-2], x[-1] (raw input before the
+ * segment), then for each section its output history y[-2], y[-1] (the filter domain after
+ * b0 / a0 normalisation, the gain applied to the input). zi = NULL starts at rest; zf = NULL
+ * skips the final state; zi and zf must not overlap. A segment with n = 0 writes nothing. */
+typedef struct {
+    const float* x;
+    float* y;
+    size_t n;
+    int filter;            /* index into the batch's filters */
+    const float* zi;
+    float* zf;
+} iir_segment;
+
+typedef struct iir_batch iir_batch;
+
+/* A batch plan over n_filters cascades: sos holds their rows back to back
+ * (sum of n_sections[f] rows of 6), n_sections[f] in 1..8. Capacities grow on demand. */
+int iir_batch_create(iir_batch** batch, const float* sos, const int* n_sections, int n_filters,
+                     size_t max_segments, size_t max_chunks);
+/* Filters every segment in one launch on `stream` (PH solve, chunks of 4096 samples, the
+ * decoupled lookback restricted to each segment). Stream-ordered; launches of one batch
+ * plan must be ordered on one stream at a time. */
+int iir_batch_execute(iir_batch* batch, const iir_segment* segs, int n_segs, void* stream);
+int iir_batch_check(iir_batch* batch, void* stream);
+int iir_batch_set_timeout_ns(iir_batch* batch, long long timeout_ns);
+int iir_batch_debug_withhold(iir_batch* batch, long long chunk);
+/* Sections of filter `filter` (the state length is 2 + 2 * sections). */
+int iir_batch_filter_sections(const iir_batch* batch, int filter);
+int iir_batch_destroy(iir_batch* batch);
+
 /* ---- helpers ------------------------------------------------------------------------- */
 const char* iir_status_string(int status);
 int iir_version(void);          /* major*10000 + minor*100 + patch */
