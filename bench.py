@@ -181,6 +181,63 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_batching(dev) -> dict:
+    """Many channels of uneven length, each with its own filter, in one launch (Batch.packed);
+    device-resident, CUDA events over 10 launches; a few channels checked against the oracle."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from cuda_recursive_filtering_gb300 import Batch, workloads
+
+    filters, lens = workloads.multichannel_mixed()
+    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 4096 + len(filters)), device=dev)
+    off = np.concatenate([[0], np.cumsum(lens)])
+    x = workloads.uniform_signal(int(off[-1]), 3, device=dev)
+    y = torch.empty_like(x)
+    flt = np.arange(len(filters), dtype=np.int32)
+    for _ in range(3):
+        batch.packed(x, y, off, flt)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+    s.record()
+    for _ in range(10):
+        batch.packed(x, y, off, flt)
+    e.record()
+    torch.cuda.synchronize()
+    batch.check()
+    ms = s.elapsed_time(e) / 10
+    worst = 0.0
+    for i in np.random.default_rng(0).choice(len(filters), 8, replace=False):
+        xi = x[off[i]:off[i + 1]].cpu().numpy()
+        _, ref = oracle.reference_golden(filters[i], xi)
+        worst = max(worst, oracle.errors(y[off[i]:off[i + 1]].cpu().numpy(), ref)["rel_max"])
+    return {"workload": "4096 channels, lengths log-uniform [2^10, 2^20], own filter each: order {2,4,8,16}, "
+                        "butter / cheby1 (1 dB), cutoff U[0.02, 0.45], seed 3; one launch",
+            "value": round(float(off[-1]) / (ms * 1e-3) / 1e9, 1), "unit": "GS/s", "ms_per_launch": ms,
+            "samples": int(off[-1]), "check_rel_max_8_channels": worst}
+
+
+def run_serving(dev, seconds: float = 2.0) -> dict:
+    """Continuous-batching stream server under Poisson arrivals (host chunks in, results back
+    on the host): achieved GS/s and request latency percentiles."""
+    from cuda_recursive_filtering_gb300 import workloads
+    from cuda_recursive_filtering_gb300.serving import StreamServer, run_poisson_load
+
+    filters, load = workloads.streaming_poisson()
+    srv = StreamServer(filters, max_batch=1024, max_streams=len(filters), device=dev, keep_outputs=False)
+    streams = [srv.open_stream(i) for i in range(len(filters))]
+    run_poisson_load(srv, streams, rate_sps=load["rate_sps"] / 4, duration_s=0.3, chunk_lo=load["chunk_lo"],
+                     chunk_hi=load["chunk_hi"], seed=1)  # warm-up
+    srv.completed.clear()
+    srv.samples_done = 0
+    out = run_poisson_load(srv, streams, rate_sps=load["rate_sps"], duration_s=seconds, chunk_lo=load["chunk_lo"],
+                           chunk_hi=load["chunk_hi"], seed=load["seed"])
+    out["workload"] = ("1024 streams, order-8 butter cutoff U[0.05, 0.4] each; chunks U[256, 65536]; "
+                       f"Poisson arrivals {load['rate_sps']:.0e} samples/s; {seconds:g} s; host chunks in and out")
+    return out
+
+
 def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     import numpy as np
     import torch
@@ -272,6 +329,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                         rows[key] = round(n / (t * 1e-3) / 1e9, 1)
                     except Exception as exc:  # report, do not hide
                         rows[key] = f"error: {exc}"
+    forms = {}
+    if not args.no_forms:
+        try:
+            forms["batching"] = run_batching(dev)
+        except Exception as exc:  # report, do not hide
+            forms["batching"] = {"error": str(exc)}
+        try:
+            forms["serving"] = run_serving(dev)
+        except Exception as exc:
+            forms["serving"] = {"error": str(exc)}
     if rank != 0:
         return
     cpu = cpu_baseline_sample(sos, x[: 1 << 24].cpu().numpy(), budget_s=args.cpu_seconds)
@@ -296,6 +363,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         "check": {"rel_max": chk["rel_max"], "rel_rms": chk["rel_rms"], "prefix_samples": m},
         "per_order_gsps": rows,
     }
+    out.update(forms)
     print(json.dumps(out), flush=True)
 
 
@@ -306,6 +374,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batching and serving legs")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")

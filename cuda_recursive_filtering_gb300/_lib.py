@@ -81,6 +81,9 @@ def load(path: str | None = None):
         "iir_batch_debug_withhold": ([vp, ll], i),
         "iir_batch_filter_sections": ([vp, i], i),
         "iir_batch_destroy": ([vp], i),
+        "iir_batch_bind": ([vp, ctypes.POINTER(IirSegment), i, pp], i),
+        "iir_batch_launch_bound": ([vp, vp], i),
+        "iir_batch_unbind": ([vp], i),
     }
     for name, (args, res) in sigs.items():
         f = getattr(L, name)

@@ -220,6 +220,73 @@ class Batch:
                                      zf.data_ptr() if zf is not None else None)
         check(self._lib.iir_batch_execute(self._ptr, arr, len(segments), _stream_handle(stream)), "iir_batch_execute")
 
+    _SEG_DTYPE = np.dtype({"names": ["x", "y", "n", "filter", "zi", "zf"],
+                           "formats": [np.uint64, np.uint64, np.uint64, np.int32, np.uint64, np.uint64],
+                           "offsets": [0, 8, 16, 24, 32, 40], "itemsize": 48})
+
+    def packed(self, x: torch.Tensor, y: torch.Tensor, offsets, filters, zi: torch.Tensor | None = None,
+               zf: torch.Tensor | None = None, stream=None) -> None:
+        """Segments packed back to back: segment i is x[offsets[i]:offsets[i+1]] -> y[...],
+        filtered with filters[i]. Optional zi / zf are (n_segments, state_len) device tensors
+        whose row i holds segment i's state (state_len = the largest state_size of the used
+        filters; rows are read / written up to the segment's own state size). The segment
+        table is built with array operations, so this path costs no per-segment Python work."""
+        _check_tensor(x, "x")
+        _check_tensor(y, "y")
+        if y.numel() != x.numel():
+            raise ValueError("y must have as many samples as x")
+        off = np.asarray(offsets, dtype=np.int64)
+        flt = np.asarray(filters, dtype=np.int32)
+        nseg = flt.size
+        tab = self._packed_table(x, y, off, flt, nseg, zi, zf)
+        self.execute_table(tab, nseg, stream)
+
+    def segment_table(self, n: int) -> np.ndarray:
+        """An empty segment table (numpy structured array laid out as iir_segment) of n rows,
+        for callers that fill pointers themselves (see execute_table)."""
+        return np.zeros(max(n, 1), dtype=self._SEG_DTYPE)
+
+    def execute_table(self, tab: np.ndarray, n: int, stream=None) -> None:
+        """Launches the first n rows of a segment table (fields x, y, n, filter, zi, zf as
+        device addresses / counts, as iir_segment)."""
+        if tab.dtype != self._SEG_DTYPE or tab.size < n:
+            raise ValueError("segment table of the wrong layout or size")
+        st = self._lib.iir_batch_execute(self._ptr, tab.ctypes.data_as(ctypes.POINTER(_lib.IirSegment)), int(n),
+                                         _stream_handle(stream))
+        check(st, "iir_batch_execute")
+
+    def bind(self, x: torch.Tensor, y: torch.Tensor, offsets, filters, zi=None, zf=None) -> "BoundBatch":
+        """Packed segments (as :meth:`packed`) uploaded once; the returned object launches
+        them with a single kernel launch per call, which CUDA graphs can capture."""
+        _check_tensor(x, "x")
+        _check_tensor(y, "y")
+        off = np.asarray(offsets, dtype=np.int64)
+        flt = np.asarray(filters, dtype=np.int32)
+        tab = self._packed_table(x, y, off, flt, flt.size, zi, zf)
+        h = ctypes.c_void_p()
+        check(self._lib.iir_batch_bind(self._ptr, tab.ctypes.data_as(ctypes.POINTER(_lib.IirSegment)), flt.size,
+                                       ctypes.byref(h)), "iir_batch_bind")
+        return BoundBatch(self, h, (x, y, zi, zf))
+
+    def _packed_table(self, x, y, off, flt, nseg, zi, zf):
+        if off.shape != (nseg + 1,) or (nseg and (off[0] < 0 or off[-1] > x.numel() or np.any(np.diff(off) < 0))):
+            raise ValueError("offsets must be nondecreasing, n_segments + 1 long, within x")
+        if nseg and (flt.min() < 0 or flt.max() >= len(self.n_sections)):
+            raise ValueError("filter index out of range")
+        tab = np.zeros(max(nseg, 1), dtype=self._SEG_DTYPE)
+        tab["x"][:nseg] = x.data_ptr() + 4 * off[:-1]
+        tab["y"][:nseg] = y.data_ptr() + 4 * off[:-1]
+        tab["n"][:nseg] = np.diff(off)
+        tab["filter"][:nseg] = flt
+        for z, name in ((zi, "zi"), (zf, "zf")):
+            if z is not None:
+                _check_tensor(z, name)
+                need = max(self.state_size(int(f)) for f in np.unique(flt)) if nseg else 0
+                if z.dim() != 2 or z.shape[0] != nseg or z.shape[1] < need:
+                    raise ValueError(f"{name} must be (n_segments, >= {need})")
+                tab[name][:nseg] = z.data_ptr() + 4 * z.shape[1] * np.arange(nseg, dtype=np.uint64)
+        return tab
+
     def check(self, stream=None) -> None:
         check(self._lib.iir_batch_check(self._ptr, _stream_handle(stream)), "device")
 
@@ -233,6 +300,29 @@ class Batch:
         if getattr(self, "_ptr", None) is not None and self._ptr.value:
             self._lib.iir_batch_destroy(self._ptr)
             self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BoundBatch:
+    """A batch's packed segments uploaded once (iir_batch_bind); calling it launches them."""
+
+    def __init__(self, batch: Batch, handle, keep):
+        self._batch = batch
+        self._h = handle
+        self._keep = keep  # the tensors the device table points into
+
+    def __call__(self, stream=None) -> None:
+        check(self._batch._lib.iir_batch_launch_bound(self._h, _stream_handle(stream)), "iir_batch_launch_bound")
+
+    def close(self) -> None:
+        if self._h is not None and self._h.value:
+            self._batch._lib.iir_batch_unbind(self._h)
+            self._h = ctypes.c_void_p()
 
     def __del__(self):
         try:

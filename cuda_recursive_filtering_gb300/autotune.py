@@ -1,0 +1,113 @@
+"""Autotuner for the plain realizations: picks realization and BLOCK_SIZE x N_BLOCKS geometry
+for a filter and signal length by timing the candidates on this GPU (CUDA events, device-
+resident data) and checking each against the FP64 reference filter on a prefix.
+
+The candidate order is a prior taken from measurements on GB300: at order 2 the two-pass
+single-section kernels, PH first; at higher orders PH with 64 samples per row. (The reference
+picks its launch shape from an occupancy model, gpu_specs.hpp:57-116; here the resident-block
+count comes from the CUDA occupancy query and the rest is measured.) Results are cached per
+(device, order, filter, signal-length bucket) in memory and, optionally, in a JSON file.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import torch
+
+from .api import Plan
+
+__all__ = ["tune", "tuned_plan"]
+
+_CANDIDATES_ORDER2 = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("STCR_UNROLL", 32, 32),
+                      ("DTCR_UNROLL", 32, 64), ("PH", 32, 128), ("PLR", 0, 0)]
+_CANDIDATES_CASCADE = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("DTCR_UNROLL", 32, 64),
+                       ("PH", 32, 128), ("STCR_UNROLL", 32, 32)]
+_memo: dict = {}
+
+
+def _key(sos: np.ndarray, n: int, device) -> str:
+    name = torch.cuda.get_device_name(device)
+    digest = np.asarray(sos, np.float32).tobytes().hex()[:32]
+    return f"{name}|{sos.shape[0]}|{digest}|{max(10, int(np.log2(max(n, 1))))}"
+
+
+def _reference_check(sos, x: np.ndarray) -> np.ndarray:
+    from scipy import signal
+    s = np.asarray(sos, np.float64)
+    return signal.sosfilt(s, x.astype(np.float64))
+
+
+def tune(sos, n: int, candidates=None, reps: int = 5, device=None, cache_path: str | None = None) -> dict:
+    """Times every candidate (realization, block_size, n_blocks) on a signal of
+    min(n, 2^26) samples and returns {"kernel", "block_size", "n_blocks", "gsps", "table"}.
+    Candidates whose output on a 2^16-sample prefix misses max|err| <= 1e-4 max|ref| (the
+    reference's gate) are skipped."""
+    sos = np.asarray(sos, dtype=np.float32).reshape(-1, 6)
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    key = _key(sos, n, dev)
+    if key in _memo:
+        return _memo[key]
+    if cache_path and os.path.exists(cache_path):
+        with open(cache_path) as f:
+            disk = json.load(f)
+        if key in disk:
+            _memo[key] = disk[key]
+            return disk[key]
+    if candidates is None:
+        candidates = _CANDIDATES_ORDER2 if sos.shape[0] == 1 else _CANDIDATES_CASCADE
+    m = int(min(max(n, 1 << 16), 1 << 26))
+    g = torch.Generator(device=dev)
+    g.manual_seed(0)
+    x = torch.rand(m, generator=g, device=dev).mul_(2).sub_(1)
+    y = torch.empty_like(x)
+    prefix = x[: 1 << 16].cpu().numpy()
+    ref = _reference_check(sos, prefix)
+    scale = float(np.max(np.abs(ref))) or 1.0
+    table = []
+    for kernel, b, nb in candidates:
+        try:
+            plan = Plan(sos, kernel, b, nb, max_n=m, device=dev)
+        except Exception:
+            continue
+        plan(x, y)
+        plan.check()
+        err = float(np.max(np.abs(y[: 1 << 16].cpu().numpy() - ref)))
+        if not np.isfinite(err) or err > 1e-4 * scale:
+            table.append({"kernel": kernel, "block_size": b, "n_blocks": nb, "gsps": None, "rejected": err / scale})
+            plan.close()
+            continue
+        for _ in range(2):
+            plan(x, y)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+        s.record()
+        for _ in range(reps):
+            plan(x, y)
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e) / reps
+        table.append({"kernel": kernel, "block_size": b, "n_blocks": nb, "gsps": m / (ms * 1e-3) / 1e9})
+        plan.close()
+    timed = [t for t in table if t["gsps"] is not None]
+    if not timed:
+        raise RuntimeError("no candidate passed the accuracy gate")
+    best = max(timed, key=lambda t: t["gsps"])
+    result = dict(best, table=table)
+    _memo[key] = result
+    if cache_path:
+        disk = {}
+        if os.path.exists(cache_path):
+            with open(cache_path) as f:
+                disk = json.load(f)
+        disk[key] = result
+        with open(cache_path, "w") as f:
+            json.dump(disk, f, indent=1)
+    return result
+
+
+def tuned_plan(sos, n: int, **kw) -> Plan:
+    """A Plan with the tuned realization and geometry for this filter and signal length."""
+    best = tune(sos, n, **{k: v for k, v in kw.items() if k in ("candidates", "reps", "device", "cache_path")})
+    return Plan(sos, best["kernel"], best["block_size"], best["n_blocks"], max_n=n, device=kw.get("device"))

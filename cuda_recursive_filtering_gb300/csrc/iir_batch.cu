@@ -504,6 +504,105 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
                                         dim3(BatchBlock::THREADS), args, BatchBlock::SMEM_BYTES, stream));
 }
 
+struct iir_batch_bound {
+    iir_batch* b = nullptr;
+    IirBatchSegment* d_segs = nullptr;
+    unsigned int* d_starts = nullptr;
+    IirBatchParams params{};
+    unsigned int nchunks = 0;
+};
+
+int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_bound** out) {
+    if (!b || !out || n_segs < 0 || (n_segs > 0 && !segs)) return IIR_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::vector<IirBatchSegment> hs(static_cast<size_t>(std::max(n_segs, 1)));
+    std::vector<unsigned int> starts(static_cast<size_t>(n_segs) + 1);
+    size_t chunk0 = 0, group0 = 0;
+    for (int i = 0; i < n_segs; ++i) {
+        const iir_segment& s = segs[i];
+        if (s.filter < 0 || s.filter >= b->n_filters) return IIR_ERR_INVALID_ARGUMENT;
+        if (s.n > 0 && (!s.x || !s.y)) return IIR_ERR_INVALID_ARGUMENT;
+        if (s.n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
+        const char* xb = reinterpret_cast<const char*>(s.x);
+        const char* yb = reinterpret_cast<const char*>(s.y);
+        if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
+        const size_t ch = (s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK;
+        hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, static_cast<unsigned int>(chunk0),
+                                static_cast<unsigned int>(group0), s.filter, 0};
+        starts[i] = static_cast<unsigned int>(chunk0);
+        chunk0 += ch;
+        group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;
+        if (chunk0 > 0x7fffffffull) return IIR_ERR_TOO_LARGE;
+    }
+    starts[n_segs] = static_cast<unsigned int>(chunk0);
+    int st = cuda_status(cudaDeviceSynchronize());
+    if (st) return st;
+    if (chunk0 > b->carry_cap || group0 > b->gcap) {
+        st = batch_alloc_carry(b, std::max(chunk0, b->carry_cap * 2), std::max<size_t>(n_segs, group0));
+        if (st) return st;
+    }
+    iir_batch_bound* h = new iir_batch_bound();
+    h->b = b;
+    h->nchunks = static_cast<unsigned int>(chunk0);
+    st = cuda_status(cudaMalloc(&h->d_segs, hs.size() * sizeof(IirBatchSegment)));
+    if (!st) st = cuda_status(cudaMalloc(&h->d_starts, starts.size() * sizeof(unsigned int)));
+    if (!st)
+        st = cuda_status(cudaMemcpy(h->d_segs, hs.data(), hs.size() * sizeof(IirBatchSegment), cudaMemcpyHostToDevice));
+    if (!st)
+        st = cuda_status(
+            cudaMemcpy(h->d_starts, starts.data(), starts.size() * sizeof(unsigned int), cudaMemcpyHostToDevice));
+    if (st) {
+        if (h->d_segs) cudaFree(h->d_segs);
+        if (h->d_starts) cudaFree(h->d_starts);
+        delete h;
+        return st;
+    }
+    IirBatchParams& q = h->params;
+    q.segs = h->d_segs;
+    q.chunk_start = h->d_starts;
+    q.filters = b->d_filters;
+    q.secs = b->d_secs;
+    q.tables = b->d_tables;
+    q.carry = b->d_carry;
+    q.state = b->d_state;
+    q.carry_stride = 4 * (b->carry_cap + b->gcap);
+    q.timeout_ns = b->timeout_ns;
+    q.withhold_chunk = -1;
+    q.nsegs = static_cast<unsigned int>(n_segs);
+    q.nchunks = h->nchunks;
+    q.carry_cap = static_cast<unsigned int>(b->carry_cap);
+    q.max_sections = b->max_sections;
+    *out = h;
+    return IIR_OK;
+}
+
+int iir_batch_launch_bound(iir_batch_bound* h, void* stream_) {
+    if (!h) return IIR_ERR_INVALID_ARGUMENT;
+    if (h->nchunks == 0) return IIR_OK;
+    iir_batch* b = h->b;
+    // the carry slots must still be the ones bound (a later execute that grew them rebinds)
+    if (h->params.carry != b->d_carry) return IIR_ERR_INVALID_ARGUMENT;
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    if (++b->launches >= (1ull << 30)) {
+        int st = cuda_status(cudaMemsetAsync(b->d_carry, 0, b->carry_bytes, stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, sizeof(IirLaunchState), stream));
+        if (st) return st;
+        b->launches = 1;
+    }
+    void* args[] = {&h->params};
+    return cuda_status(cudaLaunchKernel(reinterpret_cast<const void*>(iir_batch_kernel), dim3(h->nchunks),
+                                        dim3(BatchBlock::THREADS), args, BatchBlock::SMEM_BYTES, stream));
+}
+
+int iir_batch_unbind(iir_batch_bound* h) {
+    if (!h) return IIR_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    cudaFree(h->d_segs);
+    cudaFree(h->d_starts);
+    delete h;
+    return IIR_OK;
+}
+
 int iir_batch_check(iir_batch* b, void* stream_) {
     if (!b) return IIR_ERR_INVALID_ARGUMENT;
     cudaStream_t stream = static_cast<cudaStream_t>(stream_);

@@ -36,7 +36,7 @@ class Request:
     samples: int
     t_arrival: float
     t_done: float | None = None
-    out: torch.Tensor | None = None  # pinned host copy of the filtered chunk
+    out: torch.Tensor | None = None  # host copy of the filtered chunk (when the server keeps outputs)
 
     @property
     def latency(self) -> float | None:
@@ -44,9 +44,9 @@ class Request:
 
 
 class _Stream:
-    def __init__(self, filt: int, size: int, device):
+    def __init__(self, filt: int, slot: int):
         self.filter = filt
-        self.state = [torch.zeros(size, device=device), torch.zeros(size, device=device)]
+        self.slot = slot  # row of the server's state tensor
         self.turn = 0
         self.queue: collections.deque = collections.deque()
 
@@ -55,88 +55,134 @@ class StreamServer:
     """Continuous-batching filter service for many live streams (one GPU).
 
     ``filters``: SOS arrays (one per distinct filter). ``max_batch``: chunks per launch.
+    ``max_streams``: open streams at a time (their states live in one device tensor).
     ``reserve_bytes``: device memory left free when admitting streams and requests.
     """
 
-    def __init__(self, filters, max_batch: int = 1024, reserve_bytes: int = 1 << 30, device=None):
+    def __init__(self, filters, max_batch: int = 1024, max_streams: int = 4096, reserve_bytes: int = 1 << 30,
+                 device=None, keep_outputs: bool = True):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         with torch.cuda.device(self.device):
             self.batch = Batch(filters, max_segments=max_batch, max_chunks=1 << 16, device=self.device)
             self.cuda_stream = torch.cuda.Stream(self.device)
+            self.width = max(self.batch.state_size(f) for f in range(len(self.batch.n_sections)))
+            # [turn][slot][state]: a stream's chunk reads [turn] and writes [turn ^ 1]
+            self.states = torch.zeros(2, max_streams, self.width, device=self.device)
         self.max_batch = max_batch
+        self.max_streams = max_streams
+        self.keep_outputs = keep_outputs  # copy each request's result out of the step's pinned buffer
         self.reserve = reserve_bytes
         self.streams: dict[int, _Stream] = {}
+        self._free_slots = list(range(max_streams - 1, -1, -1))
         self._next_id = 0
         self._inflight: collections.deque = collections.deque()  # (event, requests, buffers)
+        self._pinned: list = []  # [capacity, xhost, yhost, busy until its step's results are taken]
+        self._free_bytes, self._free_t = 0, -1.0
         self.completed: list[Request] = []
         self.samples_done = 0
 
     # ---------------------------------------------------------------- admission
     def _free(self) -> int:
-        free, _ = torch.cuda.mem_get_info(self.device)
-        return free
+        # device free memory, re-read at most every 5 ms (the query is a driver call)
+        now = time.perf_counter()
+        if now - self._free_t > 5e-3:
+            self._free_bytes, _ = torch.cuda.mem_get_info(self.device)
+            self._free_t = now
+        return self._free_bytes
+
+    def _host_buffers(self, total: int):
+        # pinned input / output buffers for one step, reused once the step that used them is done
+        for entry in self._pinned:
+            if entry[0] >= total and not entry[3]:
+                entry[3] = True
+                return entry
+        cap = 1 << max(16, int(total - 1).bit_length())
+        entry = [cap, torch.empty(cap, pin_memory=True), torch.empty(cap, pin_memory=True), True]
+        self._pinned.append(entry)
+        return entry
 
     def open_stream(self, filter_index: int) -> int:
-        size = self.batch.state_size(filter_index)
-        if self._free() < self.reserve + 8 * size:
+        if not self._free_slots:
+            raise AdmissionError("stream table full")
+        if self._free() < self.reserve:
             raise AdmissionError("not enough free device memory for a new stream")
         sid = self._next_id
         self._next_id += 1
-        self.streams[sid] = _Stream(filter_index, size, self.device)
+        slot = self._free_slots.pop()
+        self.states[:, slot].zero_()
+        self.streams[sid] = _Stream(filter_index, slot)
         return sid
 
     def close_stream(self, sid: int) -> None:
-        self.streams.pop(sid)
+        s = self.streams.pop(sid)
+        self._free_slots.append(s.slot)
 
     def state(self, sid: int) -> torch.Tensor:
         """The stream's current device state (x[-2], x[-1], per section y[-2], y[-1])."""
         s = self.streams[sid]
-        return s.state[s.turn]
+        return self.states[s.turn, s.slot, :self.batch.state_size(s.filter)]
 
-    def submit(self, sid: int, chunk: np.ndarray | torch.Tensor, t_arrival: float | None = None) -> Request:
+    def submit(self, sid: int, chunk, t_arrival: float | None = None) -> Request:
         """Queues a host chunk (float32) of stream ``sid``; returns its request record."""
         s = self.streams[sid]
-        host = torch.as_tensor(np.ascontiguousarray(chunk, np.float32)) if not torch.is_tensor(chunk) else chunk
-        if self._free() < self.reserve + 8 * host.numel():
+        host = np.ascontiguousarray(chunk.numpy() if torch.is_tensor(chunk) else chunk, dtype=np.float32)
+        if self._free() < self.reserve + 8 * host.size:  # device buffers of the step: in + out
             raise AdmissionError("not enough free device memory for the request")
-        req = Request(sid, int(host.numel()), time.perf_counter() if t_arrival is None else t_arrival)
+        req = Request(sid, int(host.size), time.perf_counter() if t_arrival is None else t_arrival)
         s.queue.append((req, host))
         return req
 
     # ---------------------------------------------------------------- serving loop
     def step(self) -> int:
         """One launch over the oldest waiting chunk of every stream that has one (at most
-        ``max_batch``). Returns the number of chunks launched."""
+        ``max_batch``): one host-to-device copy of all of them, one batch launch, one copy of
+        the results back. Returns the number of chunks launched."""
         picked = []
-        for sid, s in self.streams.items():
+        for s in self.streams.values():
             if s.queue:
-                picked.append((sid, s, s.queue.popleft()))
+                picked.append(s)
                 if len(picked) == self.max_batch:
                     break
         if not picked:
             return 0
-        total = sum(req.samples for _, _, (req, _) in picked)
+        reqs, chunks = [], []
+        for s in picked:
+            req, host = s.queue.popleft()
+            reqs.append(req)
+            chunks.append(host)
+        k = len(picked)
+        lens = np.fromiter((r.samples for r in reqs), dtype=np.int64, count=k)
+        off = np.zeros(k + 1, dtype=np.int64)
+        np.cumsum(lens, out=off[1:])
+        total = int(off[-1])
+        slots = np.fromiter((s.slot for s in picked), dtype=np.int64, count=k)
+        turns = np.fromiter((s.turn for s in picked), dtype=np.int64, count=k)
+        filt = np.fromiter((s.filter for s in picked), dtype=np.int32, count=k)
+        for s in picked:
+            s.turn ^= 1
+        hb = self._host_buffers(max(total, 1))
+        xhost, yhost = hb[1][:max(total, 1)], hb[2][:max(total, 1)]
         with torch.cuda.device(self.device), torch.cuda.stream(self.cuda_stream):
+            if total:
+                np.concatenate(chunks, out=xhost.numpy()[:total])
             xin = torch.empty(max(total, 1), device=self.device)
             yout = torch.empty_like(xin)
-            yhost = torch.empty(max(total, 1), pin_memory=True)
-            segs, reqs, pos = [], [], 0
-            for sid, s, (req, host) in picked:
-                n = req.samples
-                if n:
-                    xin[pos:pos + n].copy_(host, non_blocking=True)
-                    segs.append((xin[pos:pos + n], yout[pos:pos + n], s.filter, s.state[s.turn], s.state[s.turn ^ 1]))
-                    s.turn ^= 1
-                req.out = yhost[pos:pos + n]
-                reqs.append(req)
-                pos += n
-            if segs:
-                self.batch(segs, stream=self.cuda_stream)
-            yhost[:total].copy_(yout[:total], non_blocking=True)
+            xin.copy_(xhost, non_blocking=True)
+            tab = self.batch.segment_table(k)
+            tab["x"][:k] = xin.data_ptr() + 4 * off[:-1]
+            tab["y"][:k] = yout.data_ptr() + 4 * off[:-1]
+            tab["n"][:k] = lens
+            tab["filter"][:k] = filt
+            row = 4 * self.width
+            base = self.states.data_ptr()
+            tab["zi"][:k] = base + row * (turns * self.max_streams + slots)
+            tab["zf"][:k] = base + row * ((turns ^ 1) * self.max_streams + slots)
+            self.batch.execute_table(tab, k, stream=self.cuda_stream)
+            yhost.copy_(yout, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(self.cuda_stream)
-        self._inflight.append((ev, reqs, (xin, yout, yhost)))
-        return len(reqs)
+        self._inflight.append((ev, reqs, (xin, yout, hb, off)))
+        return k
 
     def poll(self, block: bool = False) -> int:
         """Completes requests whose step has finished; returns how many completed."""
@@ -148,9 +194,14 @@ class StreamServer:
             elif not ev.query():
                 break
             t = time.perf_counter()
-            for r in reqs:
+            _, _, hb, off = self._inflight[0][2]
+            yhost = hb[2]
+            for i, r in enumerate(reqs):
                 r.t_done = t
+                if self.keep_outputs:
+                    r.out = yhost[off[i]:off[i + 1]].clone()
                 self.samples_done += r.samples
+            hb[3] = False  # results taken: the step's pinned buffers may be reused
             self.completed.extend(reqs)
             self._inflight.popleft()
             done += len(reqs)
@@ -177,6 +228,7 @@ def run_poisson_load(server: StreamServer, streams: list[int], rate_sps: float, 
     stream to a host array its chunks are taken from, in order, for correctness checks.
     Returns throughput and latency percentiles."""
     rng = np.random.default_rng(seed)
+    pool = rng.standard_normal(1 << 22).astype(np.float32)  # chunk data: slices of one pool
     mean_chunk = 0.5 * (chunk_lo + chunk_hi)
     rate_req = rate_sps / mean_chunk
     t0 = time.perf_counter()
@@ -195,7 +247,8 @@ def run_poisson_load(server: StreamServer, streams: list[int], rate_sps: float, 
                 chunk = src[p0:p0 + m]
                 positions[sid] = p0 + m
             else:
-                chunk = rng.standard_normal(m).astype(np.float32)
+                o = int(rng.integers(0, pool.size - m + 1))
+                chunk = pool[o:o + m]
             server.submit(sid, chunk, t_arrival=next_t)
             submitted += m
             next_t += rng.exponential(1.0 / rate_req)

@@ -161,6 +161,15 @@ int iir_batch_create(iir_batch** batch, const float* sos, const int* n_sections,
  * plan must be ordered on one stream at a time. */
 int iir_batch_execute(iir_batch* batch, const iir_segment* segs, int n_segs, void* stream);
 int iir_batch_check(iir_batch* batch, void* stream);
+/* A fixed segment table uploaded once (synchronously) for repeated launches: each
+ * iir_batch_launch_bound is one kernel launch and nothing else, so it can be captured into a
+ * CUDA graph and replayed. The segments' buffers must stay valid while the handle is used; an
+ * iir_batch_execute that has to grow the batch's carry slots invalidates earlier handles
+ * (iir_batch_launch_bound then returns IIR_ERR_INVALID_ARGUMENT). */
+typedef struct iir_batch_bound iir_batch_bound;
+int iir_batch_bind(iir_batch* batch, const iir_segment* segs, int n_segs, iir_batch_bound** bound);
+int iir_batch_launch_bound(iir_batch_bound* bound, void* stream);
+int iir_batch_unbind(iir_batch_bound* bound);
 int iir_batch_set_timeout_ns(iir_batch* batch, long long timeout_ns);
 int iir_batch_debug_withhold(iir_batch* batch, long long chunk);
 /* Sections of filter `filter` (the state length is 2 + 2 * sections). */

@@ -126,3 +126,59 @@ def test_batch_withheld_carry_times_out_and_recovers(cuda_device):
     batch([(xt, yt, 2)])
     batch.check()
     _check(yt.cpu().numpy(), x, filters[2][1], filters[2][0], "recovered")
+
+
+def test_packed_segments_match_list_call(cuda_device):
+    """The array-built segment table (Batch.packed) gives the same output as the list call,
+    including per-segment states in the rows of a (segments, state) tensor."""
+    filters = _filters()
+    batch = Batch([s for _, s in filters])
+    rng = np.random.default_rng(15)
+    lens = rng.integers(0, 30_000, 37)
+    off = np.concatenate([[0], np.cumsum(lens)])
+    flt = rng.integers(0, len(filters), lens.size)
+    x = torch.from_numpy(rng.uniform(-1, 1, int(off[-1])).astype(np.float32)).cuda()
+    width = max(batch.state_size(int(f)) for f in flt)
+    zi = torch.from_numpy(rng.uniform(-0.5, 0.5, (lens.size, width)).astype(np.float32)).cuda()
+    zf1 = torch.zeros_like(zi)
+    zf2 = torch.zeros_like(zi)
+    y1 = torch.empty_like(x)
+    y2 = torch.empty_like(x)
+    batch.packed(x, y1, off, flt, zi=zi, zf=zf1)
+    segs = [(x[off[i]:off[i + 1]], y2[off[i]:off[i + 1]], int(flt[i]),
+             zi[i, :batch.state_size(int(flt[i]))], zf2[i, :batch.state_size(int(flt[i]))]) for i in range(lens.size)]
+    batch(segs)
+    batch.check()
+    assert torch.allclose(y1, y2, rtol=0, atol=1e-5 * float(y2.abs().max()))
+    nz = torch.from_numpy(lens > 0).cuda()
+    assert torch.allclose(zf1[nz], zf2[nz], rtol=0, atol=1e-5 * float(zf2.abs().max() + 1))
+
+
+def test_bound_batch_replays_in_a_cuda_graph(cuda_device):
+    """A bound segment table launches with one kernel launch per call; captured into a CUDA
+    graph and replayed it gives the same output as the uncaptured launch."""
+    filters = _filters()
+    batch = Batch([s for _, s in filters])
+    rng = np.random.default_rng(16)
+    lens = rng.integers(1, 20_000, 24)
+    off = np.concatenate([[0], np.cumsum(lens)])
+    flt = rng.integers(0, len(filters), lens.size)
+    x = torch.from_numpy(rng.uniform(-1, 1, int(off[-1])).astype(np.float32)).cuda()
+    y_direct = torch.empty_like(x)
+    y_graph = torch.zeros_like(x)
+    batch.packed(x, y_direct, off, flt)
+    batch.check()
+    bound = batch.bind(x, y_graph, off, flt)
+    bound()
+    torch.cuda.synchronize()
+    assert torch.allclose(y_graph, y_direct, rtol=0, atol=1e-6 * float(y_direct.abs().max()))
+    y_graph.zero_()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        bound()
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    batch.check()
+    assert torch.allclose(y_graph, y_direct, rtol=0, atol=1e-6 * float(y_direct.abs().max()))
+    bound.close()
