@@ -22,7 +22,7 @@ IIR_ERR_OUT_OF_MEMORY = -5
 IIR_ERR_TOO_LARGE = -6
 IIR_NOALLOC_MAX_SAMPLES = 1 << 26
 
-KERNELS = {"AUTO": 0, "PH": 1, "STCR": 2, "STCR_UNROLL": 3, "DTCR": 4, "DTCR_UNROLL": 5, "PLR": 6}
+KERNELS = {"AUTO": 0, "PH": 1, "STCR": 2, "STCR_UNROLL": 3, "DTCR": 4, "DTCR_UNROLL": 5, "PLR": 6, "TC": 7}
 KERNEL_NAMES = {v: k for k, v in KERNELS.items()}
 
 

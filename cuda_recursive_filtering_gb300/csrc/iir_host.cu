@@ -256,6 +256,21 @@ bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int line
     return r == CUDA_SUCCESS;
 }
 
+// 2D tensor map over rows of row_len floats (rows x row_len), box {box_inner, box_rows},
+// 128-byte swizzle (box_inner * 4 must be 128).
+bool encode_rows_map(CUtensorMap* map, const float* base, long long rows, int row_len, int box_inner, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || rows < 1 || (reinterpret_cast<uintptr_t>(base) & 15u) || (row_len * 4) % 16) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(row_len), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(row_len) * 4};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_inner), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1u, 1u};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 // Same view with a one-line box and no swizzle: the 32 samples before a chunk.
 bool encode_hist_map(CUtensorMap* map, const float* base, long long n) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
@@ -297,6 +312,7 @@ struct iir_plan {
     size_t carry_cap = 0;      // chunks
     float4* d_tables = nullptr;
     float* d_fac = nullptr;    // PLR factor arrays
+    TcPlan* tc = nullptr;      // precision form (tensor cores)
     IirParams params{};
     IirPlrParams plr{};
     long long timeout_ns = 1000000000ll;
@@ -374,6 +390,10 @@ int plan_common_alloc(iir_plan* p, size_t max_n) {
 
 void plan_free(iir_plan* p) {
     if (!p) return;
+    if (p->tc) {
+        p->d_state = nullptr;  // owned by the precision plan
+        tc_plan_destroy(p->tc);
+    }
     if (p->d_state) cudaFree(p->d_state);
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
@@ -522,7 +542,7 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     *out = nullptr;
     if (n_sections < 1 || n_sections > IIR_MAX_SECTIONS) return IIR_ERR_INVALID_ARGUMENT;
     kernel = resolve_auto(kernel, n_sections);
-    if (kernel < IIR_KERNEL_PH || kernel > IIR_KERNEL_PLR) return IIR_ERR_INVALID_ARGUMENT;
+    if (kernel < IIR_KERNEL_PH || kernel > IIR_KERNEL_TC) return IIR_ERR_INVALID_ARGUMENT;
     std::vector<SectionF32> secs;
     double gain = 1.0;
     int st = normalise_sos(sos, n_sections, secs, gain);
@@ -531,6 +551,21 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
         std::vector<double> bt, at;
         merge_sections(secs, bt, at);
         return plan_create_plr(out, bt.data(), at.data(), 2 * n_sections, gain, block_size, n_blocks, max_n);
+    }
+    if (kernel == IIR_KERNEL_TC) {
+        iir_plan* p = new iir_plan();
+        p->kind = IIR_KIND_TC;
+        p->n_sections = n_sections;
+        st = cuda_status(cudaGetDevice(&p->device));
+        if (!st) st = tc_plan_create(&p->tc, secs.data(), n_sections, gain, max_n);
+        if (st) {
+            plan_free(p);
+            return st;
+        }
+        p->d_state = tc_plan_state(p->tc);
+        p->grid_max = tc_plan_grid(p->tc);
+        *out = p;
+        return IIR_OK;
     }
     int B = block_size, N = n_blocks;
     default_geometry(kernel, n_sections, B, N);
@@ -585,6 +620,11 @@ int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stre
     const char* yb = reinterpret_cast<const char*>(y);
     if (xb < yb + n * sizeof(float) && yb < xb + n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;  // overlap
     cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    if (p->kind == IIR_KIND_TC) {
+        const int st = tc_plan_execute(p->tc, x, y, n, p->timeout_ns, p->withhold, stream);
+        p->withhold = -1;
+        return st;
+    }
     const size_t chunk = chunk_samples(p);
     const size_t nchunks = (n + chunk - 1) / chunk;
     if (nchunks > 0xffffffffull) return IIR_ERR_TOO_LARGE;

@@ -26,7 +26,18 @@ int normalise_sos(const float* sos, int n_sections, SectionF32* out, double& gai
 int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSection& q, float4* tab);
 // 2D tensor map over a float32 signal viewed as 128-byte lines, box = lines_per_block lines.
 bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int lines_per_block);
+// 2D tensor map over rows of row_len floats, box {box_inner, box_rows}, 128-byte swizzle.
+bool encode_rows_map(CUtensorMap* map, const float* base, long long rows, int row_len, int box_inner, int box_rows);
 // cudaError_t -> IIR_* status (clears the runtime's sticky last error).
 int cuda_status(cudaError_t e);
+
+// Precision form (iir_tc.cu): the cascade's chunk solve as tensor-core GEMMs.
+struct TcPlan;
+int tc_plan_create(TcPlan** out, const SectionF32* secs, int n_sections, double gain, size_t max_n);
+int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long timeout_ns, long long withhold,
+                    cudaStream_t stream);
+IirLaunchState* tc_plan_state(TcPlan* t);
+int tc_plan_grid(const TcPlan* t);
+void tc_plan_destroy(TcPlan* t);
 
 }  // namespace iirhost

@@ -15,6 +15,7 @@ enum {
     IIR_KIND_DTCR = 4,
     IIR_KIND_DTCR_UNROLL = 5,
     IIR_KIND_PLR = 6,
+    IIR_KIND_TC = 7,
 };
 
 struct KernelEntry {

@@ -52,6 +52,8 @@ extern "C" {
 #define IIR_KERNEL_DTCR         4   /* DTCR_*_LOOP                        dtcr_kernels.cuh:291,2500 */
 #define IIR_KERNEL_DTCR_UNROLL  5   /* DTCR_*_UNROLL_*                    dtcr_kernels.cuh:660-3521 */
 #define IIR_KERNEL_PLR          6   /* PLR_2/4/8/16 direct form           plr_kernels.cuh:484-3107  */
+#define IIR_KERNEL_TC           7   /* precision form: the cascade's chunk solve as tcgen05 TF32 GEMMs
+                                       with split (3-term) products; no counterpart in the reference */
 
 typedef struct iir_plan iir_plan;
 

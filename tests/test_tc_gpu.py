@@ -1,0 +1,68 @@
+"""Precision form (IIR_KERNEL_TC): the cascade's chunk solve as tcgen05 TF32 GEMMs with split
+(3-term) products, chunk states joined by a D-dimensional scan and decoupled lookback. Against
+the FP64 oracle: max|err| <= 1e-4 * max|ref| (the reference's gate, src/test_accuracy.cu:178-188)
+and max|err| / RMS(ref) <= 1e-5 at every order (the precision form's target)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from cuda_recursive_filtering_gb300 import Plan, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(y, x, sos, rms_tol=1e-5):
+    _, ref = oracle.reference_golden(sos, x)
+    e = oracle.errors(y, ref)
+    assert e["finite"], e
+    assert e["rel_max"] <= 1e-4, e
+    assert e["rel_rms"] <= rms_tol, e
+    return e
+
+
+@pytest.mark.parametrize("order", (2, 4, 8, 16))
+def test_tc_sizes(order, cuda_device):
+    from scipy import signal
+    sos = signal.butter(order, 0.1, output="sos")
+    sizes = [1, 63, 64, 65, 8191, 8192, 8193, 3 * 8192 + 5, 160 * 8192 + 1234, (1 << 22) + 7]
+    plan = Plan(sos, "TC", max_n=max(sizes))
+    rng = np.random.default_rng(order)
+    for n in sizes:
+        x = rng.uniform(-1, 1, n).astype(np.float32)
+        y = plan(torch.from_numpy(x).cuda())
+        plan.check()
+        if n >= 64:
+            _check(y.cpu().numpy(), x, sos)
+
+
+@pytest.mark.parametrize("order", (8, 16))
+def test_tc_noise_plus_tones(order, cuda_device):
+    """butter(order, 0.05) on N(0,1) noise plus 8 sinusoids spanning 60 dB (seed 2)."""
+    from scipy import signal
+    sos = signal.butter(order, 0.05, output="sos")
+    xt = workloads.noise_plus_tones(1 << 21, 2)
+    plan = Plan(sos, "TC", max_n=xt.numel())
+    y = plan(xt)
+    plan.check()
+    _check(y.cpu().numpy(), xt.cpu().numpy(), sos)
+
+
+def test_tc_unaligned_and_repeated(cuda_device):
+    from scipy import signal
+    sos = signal.butter(8, 0.1, output="sos")
+    n = 50 * 8192 + 3
+    x = np.random.default_rng(3).uniform(-1, 1, n).astype(np.float32)
+    base = torch.zeros(n + 1, device="cuda")
+    base[1:] = torch.from_numpy(x).cuda()
+    plan = Plan(sos, "TC", max_n=n)
+    out = torch.empty(n + 1, device="cuda")[1:]
+    for _ in range(3):
+        plan(base[1:], out)  # element-wise staging (unaligned)
+    plan.check()
+    _check(out.cpu().numpy(), x, sos)
+    xt = torch.from_numpy(x).cuda()
+    for _ in range(20):
+        y = plan(xt)
+    plan.check()
+    _check(y.cpu().numpy(), x, sos)
