@@ -732,6 +732,7 @@ int iir_plan_launches_per_execute(const iir_plan* p) { return p ? 1 : 0; }
 int iir_plan_debug_profile(iir_plan* p, void* dev_buffer) {
     if (!p) return IIR_ERR_INVALID_ARGUMENT;
     p->params.prof = static_cast<unsigned long long*>(dev_buffer);
+    if (p->tc) iirhost::tc_plan_set_profile(p->tc, static_cast<unsigned long long*>(dev_buffer));
     return IIR_OK;
 }
 #endif

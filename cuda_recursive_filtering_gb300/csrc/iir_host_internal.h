@@ -37,6 +37,7 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int n_sections, double 
 int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long timeout_ns, long long withhold,
                     cudaStream_t stream);
 IirLaunchState* tc_plan_state(TcPlan* t);
+void tc_plan_set_profile(TcPlan* t, unsigned long long* buf);
 int tc_plan_grid(const TcPlan* t);
 void tc_plan_destroy(TcPlan* t);
 

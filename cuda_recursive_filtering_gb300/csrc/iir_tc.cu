@@ -35,14 +35,27 @@
 
 namespace iirgb {
 
-constexpr int TC_L = 64;                 // samples per chunk (GEMM K)
-constexpr int TC_NB = 128;               // chunks per tile (GEMM N)
-constexpr int TC_TILE = TC_L * TC_NB;    // samples per tile
-constexpr int TC_THREADS = 256;
-constexpr int TC_GROUPS = 16;            // scan sub-blocks (half-warps)
-constexpr int TC_SUB = TC_NB / TC_GROUPS;
-constexpr int TC_DMAX = 16;              // carried states (order <= 16)
-constexpr int TC_KB = 32 * 128;          // floats of one swizzled [128 rows x 32] block
+constexpr int TC_L = 64;                  // samples per chunk (GEMM K)
+constexpr int TC_NB = 128;                // chunks per tile (GEMM M)
+constexpr int TC_TILE = TC_L * TC_NB;     // samples per tile
+constexpr int TC_LBW = 2;                 // lookback warps (tiles alternate between them)
+constexpr int TC_MW = TC_LBW;             // MMA warp
+constexpr int TC_CW0 = TC_LBW + 1;        // first compute warp
+constexpr int TC_CW = 8;                  // compute warps
+constexpr int TC_CT = 32 * TC_CW;         // compute threads
+constexpr int TC_THREADS = 32 * (TC_CW0 + TC_CW);
+constexpr int TC_GROUPS = 16;             // scan sub-blocks (half-warps)
+constexpr int TC_SUB = TC_NB / TC_GROUPS;  // chunks per sub-block
+constexpr int TC_DMAX = 16;               // carried states (order <= 16)
+constexpr int TC_N1 = 80;                 // GEMM 1 N: 64 outputs + 16 end states
+constexpr int TC_N2 = 64;                 // GEMM 2 N: 64 outputs
+constexpr int TC_ACC = 80;                // TMEM columns per accumulator (3 accumulators)
+constexpr int TC_KB = 32 * TC_NB;         // floats of one swizzled [128 rows x 32] block
+constexpr int TC_B1KB = 32 * TC_N1;       // floats of one swizzled [80 rows x 32] block
+constexpr int TC_H2B = 32 * TC_N2;        // floats of one swizzled [64 rows x 32] block
+constexpr int TC_UP = 17;                 // padded row of the end-state transpose
+constexpr int TC_PP = 20;                 // padded row of an output patch
+constexpr int TC_LB_MAX = 4;              // deepest truncated lookback (tiles)
 
 struct TcParams {
     CUtensorMap tmap_x;          // x as [n/64 rows][64], box {32, 128}, 128-byte swizzle
@@ -51,11 +64,11 @@ struct TcParams {
     long long n;
     IirLaunchState* state;
     unsigned long long* carry;   // per tile slot 2*KD words, then per group of 32 tiles
-    const float* a1img;          // [hi | lo] x [2 k-blocks] x TC_KB, swizzled smem images
-    const float* a2img;          // [hi | lo] x TC_KB
+    const float* b1img;          // GEMM 1 B operand [T; B]: [hi kb0, hi kb1, lo kb0, lo kb1] x TC_B1KB
+    const float* h2img;          // GEMM 2 B operand [H | Hx]: [hi, lo] x TC_H2B
     const float* phi;            // 16 x 16 (row-major, zero beyond D)
     const float* phix;           // 16 x 2
-    const float* phi_grp;        // Phi^(8 g), g < 16: 16 x 16 x 16
+    const float* phi_pow;        // Phi^(8 * 2^b), b < 4, transposed: [b][e][d]
     const float* pc;             // Q^l (l <= 32), KD x KD
     const float* pg;             // Q^(32 l) (l <= 32), KD x KD
     long long timeout_ns;
@@ -64,32 +77,42 @@ struct TcParams {
     unsigned int carry_cap;
     int D;
     int use_tma;
+    int y_vec;                   // y is 16-byte aligned
+    int lb_depth;                // truncated lookback depth m (||Q^m|| <= 1e-10), 0: full lookback
     unsigned long long* prof;
 };
 
 struct TcAux {
-    unsigned long long mb_tma, mb_g1, mb_g2;
+    unsigned long long mb_tma[2], mb_g1, mb_g2, mb_split, mb_sready, mb_agg[TC_LBW], mb_x[TC_LBW];
     uint32_t tmem;
     uint32_t epoch;
     int bail;
-    float agg[2][TC_DMAX];           // tile aggregates (zero incoming state), per slot
-    float X[TC_DMAX];                // incoming state of the tile being finished
-    float Ag[TC_GROUPS][TC_DMAX];    // sub-block aggregates (zero start) of the current tile
-    float Ig0[2][TC_GROUPS][TC_DMAX];  // zero-start incoming state of each sub-block, per slot
-    float xh[2][TC_NB][2];           // input history of each chunk, per slot
-    float Z[2][TC_NB][TC_DMAX];      // GEMM 1 end-state rows, per slot
+    uint32_t g1_issued, g2_issued;   // MMA batches committed (by the MMA warp)
+    int pad;
+    float agg[TC_LBW][TC_DMAX];      // tile aggregate (zero incoming state) for the lookback warp
+    float X[TC_LBW][TC_DMAX];        // incoming state of the tile, from the lookback warp
+    float Ig0[2][TC_GROUPS][TC_DMAX];  // zero-start incoming state of each sub-block, per tile slot
+    float xh[3][TC_NB][2];           // input history of each chunk, per tile slot
+    float phip[4][TC_DMAX][TC_DMAX];   // Phi^(8 * 2^b), transposed
 };
 
 struct TcSmem {
-    static constexpr size_t A1 = 0;                        // hi, lo: 2 x 2 x TC_KB floats
-    static constexpr size_t A2 = A1 + 4 * TC_KB * 4;       // hi, lo: 2 x TC_KB
-    static constexpr size_t XH = A2 + 2 * TC_KB * 4;       // x tile hi (TMA target): 2 x TC_KB
-    static constexpr size_t XL = XH + 2 * TC_KB * 4;       // x tile lo
-    static constexpr size_t B2H = XL + 2 * TC_KB * 4;      // state operand hi: TC_KB
-    static constexpr size_t B2L = B2H + TC_KB * 4;         // lo
-    static constexpr size_t AUX = B2L + TC_KB * 4;
+    static constexpr size_t B1 = 0;                             // 4 x TC_B1KB floats
+    static constexpr size_t H2 = B1 + 4 * TC_B1KB * 4;          // 2 x TC_H2B
+    static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target, hi)
+    static constexpr size_t XL = XS + 4 * TC_KB * 4;            // 2 k-blocks x TC_KB (lo)
+    static constexpr size_t A2S = XL + 2 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
+    static constexpr size_t SCR = A2S + 2 * TC_KB * 4;          // scratch: transposes / output patches
+    static constexpr size_t SCR_BYTES = TC_CW * 32 * TC_PP * 4;
+    static constexpr size_t AUX = SCR + SCR_BYTES;
     static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
 };
+static_assert(TcSmem::H2 % 1024 == 0 && TcSmem::XS % 1024 == 0 && TcSmem::XL % 1024 == 0 && TcSmem::A2S % 1024 == 0,
+              "operand blocks on the 1024-byte swizzle atom");
+static_assert((TC_B1KB * 4) % 1024 == 0 && (TC_H2B * 4) % 1024 == 0, "operand blocks on the swizzle atom");
+static_assert((TC_NB * TC_UP + 2 * TC_GROUPS * TC_DMAX) * 4 <= TcSmem::SCR_BYTES, "scan scratch");
+static_assert(TcSmem::BYTES <= 232448, "shared memory");
+static_assert(3 * TC_ACC <= 256, "TMEM columns");
 
 __device__ __forceinline__ int swz32(int r, int c) { return (r << 5) + ((((c >> 2) ^ (r & 7))) << 2) + (c & 3); }
 // Nearest TF32 value of v (ties away from zero): round the magnitude at mantissa bit 13. The
@@ -102,14 +125,16 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
     return static_cast<uint64_t>((saddr >> 4) & 0x3FFF) | (static_cast<uint64_t>(1) << 16) |
            (static_cast<uint64_t>(1024 >> 4) << 32) | (static_cast<uint64_t>(1) << 46) | (static_cast<uint64_t>(2) << 61);
 }
-// kind::tf32, D f32, A / B tf32 K-major, M = 128, N = 128
-constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((TC_NB >> 3) << 17) | ((128 >> 4) << 24);
+// kind::tf32, D f32, A / B tf32 K-major, M = 128
+constexpr uint32_t tc_idesc(int n) { return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((128 >> 4) << 24); }
+constexpr uint32_t TC_IDESC1 = tc_idesc(TC_N1);
+constexpr uint32_t TC_IDESC2 = tc_idesc(TC_N2);
 
-__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t acc) {
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-        "l"(da), "l"(db), "r"(TC_IDESC), "r"(acc));
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
 __device__ __forceinline__ void umma_commit(unsigned long long* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -126,326 +151,586 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// barrier of the compute warps only (named barrier 1)
+__device__ __forceinline__ void bar_compute() { asm volatile("bar.sync 1, %0;" ::"r"(TC_CT) : "memory"); }
 
+// Optional timeline (compiled in with -DIIR_PROFILE): per block, per tile iteration k < 16,
+// 8 global-timer stamps.
+#ifdef IIR_PROFILE
+#define TC_STAMP(k, slot)                                                                                 \
+    do {                                                                                                  \
+        if (p.prof && (k) < 16u) p.prof[(static_cast<size_t>(blockIdx.x) * 16 + (k)) * 8 + (slot)] = globaltimer_ns(); \
+    } while (0)
+#else
+#define TC_STAMP(k, slot) \
+    do {                  \
+    } while (0)
+#endif
+
+// Barrier of the compute warps that also returns, to every one of them, whether any passed `v`.
+__device__ __forceinline__ bool bar_compute_any(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(static_cast<uint32_t>(v)), "r"(TC_CT)
+        : "memory");
+    return r != 0u;
+}
+
+// Bounded mbarrier wait that also gives up once another thread of the block has given up.
+__device__ __forceinline__ bool tc_wait(unsigned long long* bar, uint32_t parity, long long limit_ns, int* bail) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if ((++spins & 63u) == 0u) {
+            if (*reinterpret_cast<volatile int*>(bail)) return false;
+            if (globaltimer_ns() - t0 > static_cast<uint64_t>(limit_ns)) return false;
+        }
+    }
+    return true;
+}
+// First give-up of the block reports `code`; later ones only stop.
+__device__ __forceinline__ void tc_give_up(TcAux* aux, const TcParams& p, uint32_t epoch, uint32_t code) {
+    if (atomicExch(&aux->bail, 1) == 0) raise_error(p.state, epoch, code);
+}
+
+// Truncated lookback (one warp): X = sum_{i < m} Q^i part(t-1-i), tiles before the signal
+// contribute nothing. The neglected term Q^m X(t-m) has ||Q^m|| <= 1e-10 (checked on the host
+// in FP64), far below float32 resolution, so no chain of inclusive carries is needed: a tile
+// waits only for the aggregates of the m tiles before it. Lane i polls tile t-1-i.
+template <int KD>
+__device__ bool lookback_trunc(const TcParams& p, const unsigned long long* slots, uint32_t t, uint32_t epoch, int m,
+                               float (&X)[KD]) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t pf = 2u * epoch + 1u;
+    const bool mine = lane < m && static_cast<uint32_t>(lane) < t;
+    float v[KD];
+#pragma unroll
+    for (int e = 0; e < KD; ++e) v[e] = 0.f;
+    const uint64_t t0 = globaltimer_ns();
+    uint32_t spin = 32;
+    while (true) {
+        bool ok = true;
+        if (mine) {
+            const unsigned long long* s = slots + static_cast<size_t>(t - 1 - lane) * 2 * KD;
+#pragma unroll
+            for (int i = 0; i < KD; i += 2) {
+                unsigned long long a, b;
+                ld_relaxed_v2(s + i, a, b);
+                ok = ok && word_flag(a) == pf && word_flag(b) == pf;
+                v[i] = word_val(a);
+                v[i + 1] = word_val(b);
+            }
+        }
+        if (__all_sync(FULL_MASK, ok)) break;
+        int give_up = 0;
+        if (lane == 0) give_up = lookback_give_up(p, epoch, t0) ? 1 : 0;
+        if (__shfl_sync(FULL_MASK, give_up, 0)) return false;
+        backoff(spin);
+    }
+    float u[KD];
+    if (mine && lane > 0) {
+        matvec<KD>(p.pc + static_cast<size_t>(lane) * KD * KD, v, u);
+    } else {
+#pragma unroll
+        for (int e = 0; e < KD; ++e) u[e] = mine ? v[e] : 0.f;
+    }
+    if (m > 1) warp_sumk<KD>(u);
+#pragma unroll
+    for (int e = 0; e < KD; ++e) X[e] = __shfl_sync(FULL_MASK, u[e], 0);
+    return true;
+}
+
+// Persistent tile pipeline.
+//   warps 0 .. TC_LBW-1   lookback of alternate tiles (truncated, or the full two-level one)
+//   warp  TC_MW           tcgen05.mma issue (GEMM 1 of a staged tile, GEMM 2 of a solved one)
+//   TC_CW compute warps   per iteration k, on three tiles in flight:
+//     b. tile k:   GEMM 1 done -> end-state rows from TMEM -> sub-block scans -> aggregate -> lookback
+//     a. tile k+1: TMA data landed -> input history, TF32 split -> GEMM 1
+//     c. tile k-1: lookback's X -> states of its chunks -> GEMM 2
+//     d. tile k-1: GEMM 2 done -> outputs from TMEM -> y
+// The lookback of tile k runs while the compute warps do a(k+1) .. b(k+1); TMEM holds three
+// accumulators (tiles k-1, k, k+1); x is double-buffered (TMA two tiles ahead).
 template <int KD>
 __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_constant__ TcParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t a0 = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((a0 + 1023u) & ~1023u) - a0);
-    float* a1 = reinterpret_cast<float*>(base + TcSmem::A1);
-    float* a2 = reinterpret_cast<float*>(base + TcSmem::A2);
-    float* xhb = reinterpret_cast<float*>(base + TcSmem::XH);
-    float* xlb = reinterpret_cast<float*>(base + TcSmem::XL);
-    float* b2h = reinterpret_cast<float*>(base + TcSmem::B2H);
-    float* b2l = reinterpret_cast<float*>(base + TcSmem::B2L);
+    float* b1 = reinterpret_cast<float*>(base + TcSmem::B1);
+    float* h2 = reinterpret_cast<float*>(base + TcSmem::H2);
+    float* xs = reinterpret_cast<float*>(base + TcSmem::XS);
+    float* xl = reinterpret_cast<float*>(base + TcSmem::XL);
+    float* a2s = reinterpret_cast<float*>(base + TcSmem::A2S);
+    float* scr = reinterpret_cast<float*>(base + TcSmem::SCR);
     TcAux* aux = reinterpret_cast<TcAux*>(base + TcSmem::AUX);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int D = p.D;
     const uint32_t G = gridDim.x;
     const uint32_t nk = (p.ntiles > blockIdx.x) ? (p.ntiles - blockIdx.x + G - 1) / G : 0;
+    const long long wait_lim = p.timeout_ns < (1ll << 60) ? 4 * p.timeout_ns : p.timeout_ns;
 
-    // ---- setup: operand images, zeroed state operand, TMEM, barriers ----
+    // ---- setup: operand images, matrix powers, zeroed state operand, TMEM, barriers ----
     {
-        const float4* s1 = reinterpret_cast<const float4*>(p.a1img);
-        float4* d1 = reinterpret_cast<float4*>(a1);
-        for (int i = tid; i < TC_KB; i += TC_THREADS) d1[i] = __ldg(s1 + i);  // 4 blocks = TC_KB float4
-        const float4* s2 = reinterpret_cast<const float4*>(p.a2img);
-        float4* d2 = reinterpret_cast<float4*>(a2);
-        for (int i = tid; i < TC_KB / 2; i += TC_THREADS) d2[i] = __ldg(s2 + i);
-        float4* z = reinterpret_cast<float4*>(b2h);
-        for (int i = tid; i < TC_KB / 2; i += TC_THREADS) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // b2h, b2l
+        const float4* s1 = reinterpret_cast<const float4*>(p.b1img);
+        float4* d1 = reinterpret_cast<float4*>(b1);
+        for (int i = tid; i < TC_B1KB; i += TC_THREADS) d1[i] = __ldg(s1 + i);  // 4 x TC_B1KB floats
+        const float4* s2 = reinterpret_cast<const float4*>(p.h2img);
+        float4* d2 = reinterpret_cast<float4*>(h2);
+        for (int i = tid; i < TC_H2B / 2; i += TC_THREADS) d2[i] = __ldg(s2 + i);  // 2 x TC_H2B floats
+        float4* z = reinterpret_cast<float4*>(a2s);
+        for (int i = tid; i < TC_KB / 2; i += TC_THREADS) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // 2 x TC_KB
+        float* pp = &aux->phip[0][0][0];
+        for (int i = tid; i < 4 * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
     }
-    if (warp == 0) {
+    if (warp == TC_MW) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&aux->tmem)),
                      "r"(256));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 32) {
-        mbar_init(&aux->mb_tma, 1);
+    if (tid == 0) {
+        mbar_init(&aux->mb_tma[0], 1);
+        mbar_init(&aux->mb_tma[1], 1);
         mbar_init(&aux->mb_g1, 1);
         mbar_init(&aux->mb_g2, 1);
+        mbar_init(&aux->mb_split, 1);
+        mbar_init(&aux->mb_sready, 1);
+        for (int w = 0; w < TC_LBW; ++w) {
+            mbar_init(&aux->mb_agg[w], 1);
+            mbar_init(&aux->mb_x[w], 1);
+        }
         fence_mbar_init();
         aux->epoch = static_cast<uint32_t>(*reinterpret_cast<volatile unsigned long long*>(&p.state->ticket) >> 32);
         aux->bail = 0;
+        aux->g1_issued = aux->g2_issued = 0;
     }
     fence_proxy_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = aux->tmem, epoch = aux->epoch;
-
-    // this thread's state row d of Phi, Phix (scan: half-warp groups, lane d = state component)
-    const int grp = tid >> 4, d = tid & 15;
-    float phi_row[TC_DMAX], phix_row[2];
-#pragma unroll
-    for (int e = 0; e < TC_DMAX; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
-    phix_row[0] = __ldg(p.phix + d * 2);
-    phix_row[1] = __ldg(p.phix + d * 2 + 1);
-
     unsigned long long* slots = p.carry;
     unsigned long long* gslots = p.carry + static_cast<size_t>(p.carry_cap) * 2 * KD;
-    const uint32_t pf = 2u * epoch + 1u, ff = 2u * epoch + 2u;
-    uint32_t ph_tma = 0, ph_g1 = 0, ph_g2 = 0;
-    bool live1 = false, pend1 = false, pend2 = false;
+    volatile int* vbail = &aux->bail;
 
-    for (uint32_t k = 0; k <= nk; ++k) {
-        const int slot = k & 1;
-        const uint32_t t = blockIdx.x + k * G;  // tile of this iteration (k < nk)
-        if (k < nk) {
-            // ---- 1. load the tile (chunks as rows, samples as K) and split it hi / lo ----
-            const long long ts = static_cast<long long>(t) * TC_TILE;
-            const bool bulk = p.use_tma && ts + TC_TILE <= p.n;
-            if (bulk) {
-                if (tid == 0) {
-                    mbar_arrive_expect_tx(&aux->mb_tma, 2u * TC_KB * 4u);
-                    tma_load_2d(xhb, &p.tmap_x, 0, static_cast<int>(t) * TC_NB, &aux->mb_tma);
-                    tma_load_2d(xhb + TC_KB, &p.tmap_x, 32, static_cast<int>(t) * TC_NB, &aux->mb_tma);
-                }
-                if (!wait_mbar_bounded(&aux->mb_tma, ph_tma, p.timeout_ns) && tid == 0) {
-                    aux->bail = 1;
-                    raise_error(p.state, epoch, IIR_DEV_ERR_MBARRIER);
-                }
-                ph_tma ^= 1u;
-            } else {
-                for (int i = tid; i < TC_TILE; i += TC_THREADS) {
-                    const int j = i / TC_L, c = i % TC_L;
-                    const long long g = ts + i;
-                    xhb[(c >> 5) * TC_KB + swz32(j, c & 31)] = (g < p.n) ? p.x[g] : 0.f;
-                }
+    if (warp < TC_LBW) {
+        // ================= lookback warps: tiles k = warp, warp + TC_LBW, ... =================
+        const uint32_t ff = 2u * epoch + 2u;
+        for (uint32_t k = warp; k < nk; k += TC_LBW) {
+            const uint32_t par = (k / TC_LBW) & 1u;
+            int got = 0;
+            if (lane == 0) {
+                got = tc_wait(&aux->mb_agg[warp], par, wait_lim, &aux->bail) ? 1 : 0;
+                if (!got) tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                else if (*vbail) got = 0;
             }
-            __syncthreads();
-            // input history of each chunk: the two samples before it
-            if (tid < TC_NB) {
-                float h2, h1;
-                if (tid > 0) {
-                    h2 = xhb[TC_KB + swz32(tid - 1, 30)];
-                    h1 = xhb[TC_KB + swz32(tid - 1, 31)];
-                } else if (ts > 0) {
-                    h2 = p.x[ts - 2];
-                    h1 = p.x[ts - 1];
-                } else {
-                    h2 = h1 = 0.f;
+            __syncwarp();
+            if (!__shfl_sync(FULL_MASK, got, 0)) break;
+            const uint32_t t = blockIdx.x + k * G;
+            if (lane == 0) TC_STAMP(k, 6);
+            float own[KD], X[KD];
+#pragma unroll
+            for (int e = 0; e < KD; ++e) {
+                own[e] = aux->agg[warp][e];
+                X[e] = 0.f;
+            }
+            const bool withhold = static_cast<long long>(t) == p.withhold_chunk;
+            bool ok = true;
+            if (p.lb_depth > 0) {
+                if (t > 0) ok = lookback_trunc<KD>(p, slots, t, epoch, p.lb_depth, X);
+            } else if (t > 0) {
+                ok = lookback_hier_k<KD>(p, slots, gslots, p.pc, p.pg, t, epoch, own, withhold, X);
+            }
+            if (lane == 0) {
+                if (ok && !withhold && p.lb_depth == 0) {
+                    float f[KD];
+                    matvec<KD>(p.pc + KD * KD, X, f);  // Q X
+#pragma unroll
+                    for (int e = 0; e < KD; ++e) f[e] += own[e];
+                    publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD + KD, ff, f);
+                    if ((t & 31u) == 31u) publishk<KD>(gslots + static_cast<size_t>(t >> 5) * 2 * KD + KD, ff, f);
                 }
-                aux->xh[slot][tid][0] = h2;
-                aux->xh[slot][tid][1] = h1;
+                if (!ok) atomicExch(&aux->bail, 1);  // the lookback has reported its timeout
+#pragma unroll
+                for (int e = 0; e < TC_DMAX; ++e) aux->X[warp][e] = e < KD ? X[e] : 0.f;
+                mbar_arrive(&aux->mb_x[warp]);
+                TC_STAMP(k, 7);
             }
-            __syncthreads();
-            for (int i = tid; i < 2 * TC_KB; i += TC_THREADS) {
-                const float v = xhb[i];
-                const float h = tf32_hi(v);
-                xhb[i] = h;
-                xlb[i] = tf32_hi(v - h);
-            }
-            fence_proxy_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            live1 = !aux->bail;  // every thread reads it after the same barrier
-            // ---- 2. GEMM 1: [T; B] X -> TMEM slot ----
-            if (tid == 0 && live1) {
-                const uint32_t dt = tmem + slot * TC_NB;
+            __syncwarp();
+            if (!ok) break;
+        }
+    } else if (warp == TC_MW) {
+        // ================= MMA warp: the compute warps' order, a(k+1) then c(k-1) =================
+        if (lane == 0) {
+            uint32_t n_split = 0, n_sready = 0;
+            auto gemm1 = [&](uint32_t kk) {
+                if (!tc_wait(&aux->mb_split, n_split & 1u, wait_lim, &aux->bail)) return false;
+                ++n_split;
+                tc_fence_after();
+                const float* xt = xs + (kk & 1) * 2 * TC_KB;
+                const uint32_t dt = tmem + static_cast<uint32_t>((kk % 3) * TC_ACC);
                 uint32_t acc = 0;
 #pragma unroll
                 for (int kb = 0; kb < 2; ++kb) {
 #pragma unroll
                     for (int ks = 0; ks < 4; ++ks) {
                         const uint32_t oa = (kb * TC_KB) * 4 + ks * 32;
-                        const uint64_t ah = umma_desc(smem_u32(a1) + oa);
-                        const uint64_t al = umma_desc(smem_u32(a1) + 2 * TC_KB * 4 + oa);
-                        const uint64_t bh = umma_desc(smem_u32(xhb) + oa);
-                        const uint64_t bl = umma_desc(smem_u32(xlb) + oa);
-                        umma_tf32(dt, ah, bh, acc);
-                        umma_tf32(dt, ah, bl, 1u);
-                        umma_tf32(dt, al, bh, 1u);
+                        const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
+                        const uint64_t ah = umma_desc(smem_u32(xt) + oa);
+                        const uint64_t al = umma_desc(smem_u32(xl) + oa);
+                        const uint64_t bh = umma_desc(smem_u32(b1) + ob);
+                        const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
+                        umma_tf32(dt, ah, bh, TC_IDESC1, acc);
+                        umma_tf32(dt, ah, bl, TC_IDESC1, 1u);
+                        umma_tf32(dt, al, bh, TC_IDESC1, 1u);
                         acc = 1u;
                     }
                 }
                 umma_commit(&aux->mb_g1);
-            }
-        }
-        // ---- 3. lookback of the previous tile (its aggregate was published one iteration ago) ----
-        if (k >= 1 && warp == 0) {
-            const uint32_t tp = blockIdx.x + (k - 1) * G;
-            float own[KD], X[KD];
+                ++aux->g1_issued;
+                return true;
+            };
+            auto gemm2 = [&](uint32_t kk) {
+                if (!tc_wait(&aux->mb_sready, n_sready & 1u, wait_lim, &aux->bail)) return false;
+                ++n_sready;
+                tc_fence_after();
+                const uint32_t dt = tmem + static_cast<uint32_t>((kk % 3) * TC_ACC);
 #pragma unroll
-            for (int e = 0; e < KD; ++e) {
-                own[e] = aux->agg[slot ^ 1][e];
-                X[e] = 0.f;
-            }
-            const bool withhold = static_cast<long long>(tp) == p.withhold_chunk;
-            bool ok = true;
-            if (tp > 0 && !aux->bail) ok = lookback_hier_k<KD>(p, slots, gslots, p.pc, p.pg, tp, epoch, own, withhold, X);
-            if (lane == 0) {
-                if (ok && !withhold && !aux->bail) {
-                    float f[KD];
-                    matvec<KD>(p.pc + KD * KD, X, f);  // Q X
-#pragma unroll
-                    for (int e = 0; e < KD; ++e) f[e] += own[e];
-                    publishk<KD>(slots + static_cast<size_t>(tp) * 2 * KD + KD, ff, f);
-                    if ((tp & 31u) == 31u) publishk<KD>(gslots + static_cast<size_t>(tp >> 5) * 2 * KD + KD, ff, f);
+                for (int ks = 0; ks < 4; ++ks) {
+                    const uint32_t o = ks * 32;
+                    const uint64_t ah = umma_desc(smem_u32(a2s) + o);
+                    const uint64_t al = umma_desc(smem_u32(a2s) + TC_KB * 4 + o);
+                    const uint64_t bh = umma_desc(smem_u32(h2) + o);
+                    const uint64_t bl = umma_desc(smem_u32(h2) + TC_H2B * 4 + o);
+                    umma_tf32(dt, ah, bh, TC_IDESC2, 1u);
+                    umma_tf32(dt, ah, bl, TC_IDESC2, 1u);
+                    umma_tf32(dt, al, bh, TC_IDESC2, 1u);
                 }
-                if (!ok) aux->bail = 1;
-#pragma unroll
-                for (int e = 0; e < TC_DMAX; ++e) aux->X[e] = e < KD ? X[e] : 0.f;
+                umma_commit(&aux->mb_g2);
+                ++aux->g2_issued;
+                return true;
+            };
+            bool go = nk == 0 || gemm1(0);
+            for (uint32_t k = 0; go && k <= nk; ++k) {
+                if (k + 1 < nk) go = gemm1(k + 1);
+                if (go && k >= 1) go = gemm2(k - 1);
             }
         }
-        if (k < nk) {
-            // ---- 4. GEMM 1 done: end-state rows (TMEM lanes 64 ..) to shared memory ----
-            if (live1) {
-                if (!wait_mbar_bounded(&aux->mb_g1, ph_g1, p.timeout_ns)) {
-                    pend1 = true;  // waited for again (bounded) before TMEM is freed
-                    if (tid == 0) {
-                        aux->bail = 1;
-                        raise_error(p.state, epoch, IIR_DEV_ERR_MBARRIER);
-                    }
+        __syncwarp();
+    } else {
+        // ================= compute warps =================
+        const int ct = tid - 32 * TC_CW0;       // 0 .. TC_CT-1
+        const int cw = warp - TC_CW0;           // 0 .. TC_CW-1
+        const int q = warp & 3;                 // TMEM lane quadrant of this warp
+        const int hh = cw >> 2;                 // which of the two warps on the quadrant
+        const int grp = ct >> 4, d = ct & 15;   // scan: sub-block, state component
+        float phi_row[KD], phix0, phix1;
+#pragma unroll
+        for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
+        phix0 = __ldg(p.phix + d * 2);
+        phix1 = __ldg(p.phix + d * 2 + 1);
+        float* U = scr;                                   // [128][TC_UP] end-state rows
+        float* V0 = scr + TC_NB * TC_UP;                  // [16][16] x 2 combine ping-pong
+        float* V1 = V0 + TC_GROUPS * TC_DMAX;
+        // Waits count completed phases (every compute thread waits on every phase); ct == 0
+        // issues the TMA loads and counts them, for the drain at the end.
+        uint32_t tma_par[2] = {0u, 0u}, g1_par = 0, g2_par = 0;
+        uint32_t tma_real[2] = {0u, 0u};
+
+        auto tile_of = [&](uint32_t kk) { return blockIdx.x + kk * G; };
+        auto bulk = [&](uint32_t kk) {
+            return p.use_tma && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
+        };
+        auto issue_tma = [&](uint32_t kk) {  // by ct == 0
+            const int s = kk & 1;
+            float* dst = xs + s * 2 * TC_KB;
+            mbar_arrive_expect_tx(&aux->mb_tma[s], 2u * TC_KB * 4u);
+            tma_load_2d(dst, &p.tmap_x, 0, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[s]);
+            tma_load_2d(dst + TC_KB, &p.tmap_x, 32, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[s]);
+            ++tma_real[s];
+        };
+        // TMEM address of accumulator slot s, this warp's lane quadrant, column c
+        auto tacc = [&](int s, int c) {
+            return tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(s * TC_ACC + c);
+        };
+        // end-state rows of tile kk (TMEM columns 64 ..) -> U[chunk][state]
+        auto load_z = [&](uint32_t kk) {
+            float v[8];
+            __syncwarp();
+            tmem_ld8(tacc(kk % 3, 64 + 8 * hh), v);
+            float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) u[i] = v[i];
+        };
+        // one recurrence step of the half-warp's state: Phi S + Z_j + Phix xh_j
+        auto step = [&](float S, int j, const float* xhj) {
+            float s0 = U[j * TC_UP + d], s1 = phix0 * xhj[0], s2 = phix1 * xhj[1], s3 = 0.f;
+#pragma unroll
+            for (int e = 0; e < KD; e += 4) {
+                s0 = fmaf(phi_row[e], __shfl_sync(0xffffffffu, S, e, 16), s0);
+                if (e + 1 < KD) s1 = fmaf(phi_row[e + 1], __shfl_sync(0xffffffffu, S, e + 1, 16), s1);
+                if (e + 2 < KD) s2 = fmaf(phi_row[e + 2], __shfl_sync(0xffffffffu, S, e + 2, 16), s2);
+                if (e + 3 < KD) s3 = fmaf(phi_row[e + 3], __shfl_sync(0xffffffffu, S, e + 3, 16), s3);
+            }
+            return (s0 + s1) + (s2 + s3);
+        };
+        // y_d = sum_e M[d][e] v_e with M = Phi^(8 * 2^b) (transposed in shared memory), v a
+        // vector in shared memory
+        auto mv_smem = [&](int b, const float* v) {
+            const float* mt = &aux->phip[b][0][0];
+            float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+            for (int e = 0; e < KD; e += 2) {
+                s0 = fmaf(mt[e * TC_DMAX + d], v[e], s0);
+                if (e + 1 < KD) s1 = fmaf(mt[(e + 1) * TC_DMAX + d], v[e + 1], s1);
+            }
+            return s0 + s1;
+        };
+        // stage tile kk: data landed (TMA) or gathered, input history, TF32 split, then hand
+        // it to the MMA warp. Returns the block's stop decision (the same in every compute thread).
+        auto stage_tile = [&](uint32_t kk) {
+            const int s = kk & 1;
+            float* xt = xs + s * 2 * TC_KB;
+            const long long ts = static_cast<long long>(tile_of(kk)) * TC_TILE;
+            if (bulk(kk)) {
+                if (tc_wait(&aux->mb_tma[s], tma_par[s] & 1u, p.timeout_ns, &aux->bail))
+                    ++tma_par[s];
+                else
+                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+            } else {
+                for (int i = ct; i < TC_TILE; i += TC_CT) {
+                    const int j = i / TC_L, c = i % TC_L;
+                    const long long g = ts + i;
+                    xt[(c >> 5) * TC_KB + swz32(j, c & 31)] = (g < p.n) ? p.x[g] : 0.f;
+                }
+                bar_compute();
+            }
+            if (ct < TC_NB) {  // the two samples before each chunk
+                float x2, x1;
+                if (ct > 0) {
+                    x2 = xt[TC_KB + swz32(ct - 1, 30)];
+                    x1 = xt[TC_KB + swz32(ct - 1, 31)];
+                } else if (ts > 0) {
+                    x2 = p.x[ts - 2];
+                    x1 = p.x[ts - 1];
                 } else {
-                    ph_g1 ^= 1u;
+                    x2 = x1 = 0.f;
                 }
+                aux->xh[kk % 3][ct][0] = x2;
+                aux->xh[kk % 3][ct][1] = x1;
             }
-            tc_fence_after();
-            if (warp == 2 && !aux->bail) {
-                for (int c = 0; c < TC_NB; c += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + (64u << 16) + slot * TC_NB + c, v);
-                    if (lane < TC_DMAX) {
-#pragma unroll
-                        for (int i = 0; i < 16; ++i) aux->Z[slot][c + i][lane] = lane < D ? v[i] : 0.f;
-                    }
-                }
+            bar_compute();
+            float4* h4 = reinterpret_cast<float4*>(xt);
+            float4* l4 = reinterpret_cast<float4*>(xl);
+            for (int i = ct; i < TC_KB / 2; i += TC_CT) {  // 2 k-blocks x TC_KB floats
+                const float4 v = h4[i];
+                float4 h, l;
+                h.x = tf32_hi(v.x);
+                h.y = tf32_hi(v.y);
+                h.z = tf32_hi(v.z);
+                h.w = tf32_hi(v.w);
+                l.x = tf32_hi(v.x - h.x);
+                l.y = tf32_hi(v.y - h.y);
+                l.z = tf32_hi(v.z - h.z);
+                l.w = tf32_hi(v.w - h.w);
+                h4[i] = h;
+                l4[i] = l;
             }
-            __syncthreads();
-            // ---- 5. scan from zero: sub-block aggregates, then the tile aggregate ----
-            {
-                float S = 0.f;
-                for (int i = 0; i < TC_SUB; ++i) {
-                    const int j = grp * TC_SUB + i;
-                    float acc = aux->Z[slot][j][d];
-                    acc = fmaf(phix_row[0], aux->xh[slot][j][0], acc);
-                    acc = fmaf(phix_row[1], aux->xh[slot][j][1], acc);
-#pragma unroll
-                    for (int e = 0; e < TC_DMAX; ++e) acc = fmaf(phi_row[e], __shfl_sync(FULL_MASK, S, e, 16), acc);
-                    S = acc;
-                }
-                aux->Ag[grp][d] = S;
-            }
-            __syncthreads();
-            if (grp == 0) {
-                // zero-start incoming state of every sub-block: I_{g+1} = Phi^8 I_g + A_g
-                const float* p8 = p.phi_grp + 1 * TC_DMAX * TC_DMAX;  // Phi^8
-                float I = 0.f;
-                for (int g = 0; g < TC_GROUPS; ++g) {
-                    aux->Ig0[slot][g][d] = I;
-                    float acc = aux->Ag[g][d];
-#pragma unroll
-                    for (int e = 0; e < TC_DMAX; ++e)
-                        acc = fmaf(__ldg(p8 + d * TC_DMAX + e), __shfl_sync(0x0000ffffu, I, e, 16), acc);
-                    I = acc;
-                }
-                aux->agg[slot][d] = I;
-            }
-            __syncthreads();
-            if (tid == 0 && static_cast<long long>(t) != p.withhold_chunk) {
-                float a[KD];
-#pragma unroll
-                for (int e = 0; e < KD; ++e) a[e] = aux->agg[slot][e];
-                publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD, pf, a);
-            }
-        } else {
-            __syncthreads();  // the lookback's X is visible
+            fence_proxy_async_smem();
+            tc_fence_before();
+            const bool stop = bar_compute_any(*vbail);
+            if (!stop && ct == 0) mbar_arrive(&aux->mb_split);
+            return stop;
+        };
+
+        // prologue: data of the first two tiles, tile 0 staged
+        if (ct == 0) {
+            for (uint32_t kk = 0; kk < 2 && kk < nk; ++kk)
+                if (bulk(kk)) issue_tma(kk);
         }
-        // ---- 6. finish the previous tile: states, GEMM 2, output ----
-        if (k >= 1) {
-            __syncthreads();
-            const int ps = slot ^ 1;
-            const uint32_t tp = blockIdx.x + (k - 1) * G;
-            if (!aux->bail) {
-                // true incoming state of the sub-block, then its chunks' states into the operand
-                const float* pgm = p.phi_grp + static_cast<size_t>(grp) * TC_DMAX * TC_DMAX;
-                float S = aux->Ig0[ps][grp][d];
+        bool stop = nk > 0 ? stage_tile(0) : false;
+
+        for (uint32_t k = 0; k <= nk && !stop; ++k) {
+            if (ct == 0) TC_STAMP(k, 0);
+            // ---- b. tile k: sub-block scans, tile aggregate, hand-off to the lookback warp ----
+            if (k < nk) {
+                if (tc_wait(&aux->mb_g1, g1_par & 1u, p.timeout_ns, &aux->bail))
+                    ++g1_par;
+                else
+                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                tc_fence_after();
+                if (ct == 0 && k + 2 < nk && bulk(k + 2) && !*vbail) issue_tma(k + 2);  // its stage is free
+                load_z(k);
+                if (bar_compute_any(*vbail)) break;
+                const float* xhk = &aux->xh[k % 3][0][0];
+                float S = 0.f;
+                for (int i = 0; i < TC_SUB; ++i) S = step(S, grp * TC_SUB + i, xhk + (grp * TC_SUB + i) * 2);
+                V0[grp * TC_DMAX + d] = S;
+                bar_compute();
+                // inclusive scan over the sub-blocks: V_g += Phi^(8 s) V_(g-s), s = 1, 2, 4, 8
+                float* Vc = V0;
+                float* Vn = V1;
 #pragma unroll
-                for (int e = 0; e < TC_DMAX; ++e) S = fmaf(__ldg(pgm + d * TC_DMAX + e), aux->X[e], S);
+                for (int l = 0; l < 4; ++l) {
+                    const int s = 1 << l;
+                    float a = Vc[grp * TC_DMAX + d];
+                    if (grp >= s) a += mv_smem(l, Vc + (grp - s) * TC_DMAX);
+                    Vn[grp * TC_DMAX + d] = a;
+                    bar_compute();
+                    float* tsw = Vc;
+                    Vc = Vn;
+                    Vn = tsw;
+                }
+                aux->Ig0[k & 1][grp][d] = grp > 0 ? Vc[(grp - 1) * TC_DMAX + d] : 0.f;
+                if (grp == TC_GROUPS - 1) aux->agg[k % TC_LBW][d] = Vc[grp * TC_DMAX + d];
+                bar_compute();
+                if (ct == 0) {
+                    const uint32_t t = tile_of(k);
+                    if (static_cast<long long>(t) != p.withhold_chunk) {
+                        float a[KD];
+#pragma unroll
+                        for (int e = 0; e < KD; ++e) a[e] = aux->agg[k % TC_LBW][e];
+                        publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD, 2u * epoch + 1u, a);
+                    }
+                    mbar_arrive(&aux->mb_agg[k % TC_LBW]);
+                    TC_STAMP(k, 1);
+                }
+            }
+            // ---- a. tile k+1: stage (GEMM 1 of tile k has read the lo buffer) ----
+            if (k + 1 < nk) {
+                stop = stage_tile(k + 1);
+                if (stop) break;
+            }
+            if (ct == 0) TC_STAMP(k, 2);
+            // ---- c. tile k-1: states of its chunks, then GEMM 2 ----
+            if (k >= 1) {
+                const uint32_t kp = k - 1, sl = kp % TC_LBW;
+                if (!tc_wait(&aux->mb_x[sl], (kp / TC_LBW) & 1u, wait_lim, &aux->bail))
+                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                if (ct == 0) TC_STAMP(k, 3);
+                load_z(kp);
+                // incoming state of the sub-block: Ig0 + Phi^(8 grp) X, Phi^(8 grp) as a product of
+                // Phi^(8 * 2^b) over the bits of grp (the vector goes through the scratch V0)
+                float* vx = V0 + grp * TC_DMAX;
+                vx[d] = aux->X[sl][d];
+                __syncwarp();
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const float w = mv_smem(b, vx);
+                    __syncwarp();
+                    if ((grp >> b) & 1) vx[d] = w;
+                    __syncwarp();
+                }
+                const float xin = vx[d];
+                if (bar_compute_any(*vbail)) break;
+                const float* xhp = &aux->xh[kp % 3][0][0];
+                float S = aux->Ig0[kp & 1][grp][d] + xin;
                 for (int i = 0; i < TC_SUB; ++i) {
                     const int j = grp * TC_SUB + i;
                     if (d < D) {
                         const float h = tf32_hi(S);
-                        b2h[swz32(j, d)] = h;
-                        b2l[swz32(j, d)] = tf32_hi(S - h);
-                    }
-                    if (d < 2) {  // the chunk's input history in columns D, D + 1
-                        const float v = aux->xh[ps][j][d];
+                        a2s[swz32(j, d)] = h;
+                        a2s[TC_KB + swz32(j, d)] = tf32_hi(S - h);
+                    } else if (d < D + 2) {  // the chunk's input history in columns D, D + 1
+                        const float v = xhp[j * 2 + (d - D)];
                         const float h = tf32_hi(v);
-                        b2h[swz32(j, D + d)] = h;
-                        b2l[swz32(j, D + d)] = tf32_hi(v - h);
+                        a2s[swz32(j, d)] = h;
+                        a2s[TC_KB + swz32(j, d)] = tf32_hi(v - h);
                     }
-                    float acc = aux->Z[ps][j][d];
-                    acc = fmaf(phix_row[0], aux->xh[ps][j][0], acc);
-                    acc = fmaf(phix_row[1], aux->xh[ps][j][1], acc);
-#pragma unroll
-                    for (int e = 0; e < TC_DMAX; ++e) acc = fmaf(phi_row[e], __shfl_sync(FULL_MASK, S, e, 16), acc);
-                    S = acc;
+                    S = step(S, j, xhp + j * 2);
                 }
-            }
-            fence_proxy_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            const bool live2 = !aux->bail;
-            if (tid == 0 && live2) {
-                const uint32_t dt = tmem + ps * TC_NB;
-#pragma unroll
-                for (int ks = 0; ks < 4; ++ks) {
-                    const uint32_t o = ks * 32;
-                    const uint64_t ah = umma_desc(smem_u32(a2) + o);
-                    const uint64_t al = umma_desc(smem_u32(a2) + TC_KB * 4 + o);
-                    const uint64_t bh = umma_desc(smem_u32(b2h) + o);
-                    const uint64_t bl = umma_desc(smem_u32(b2l) + o);
-                    umma_tf32(dt, ah, bh, 1u);
-                    umma_tf32(dt, ah, bl, 1u);
-                    umma_tf32(dt, al, bh, 1u);
-                }
-                umma_commit(&aux->mb_g2);
-            }
-            if (live2) {
-                if (!wait_mbar_bounded(&aux->mb_g2, ph_g2, p.timeout_ns)) {
-                    pend2 = true;
-                    if (tid == 0) {
-                        aux->bail = 1;
-                        raise_error(p.state, epoch, IIR_DEV_ERR_MBARRIER);
-                    }
-                } else {
-                    ph_g2 ^= 1u;
-                }
-            }
-            tc_fence_after();
-            if (warp < 2 && !aux->bail) {
-                const long long ts = static_cast<long long>(tp) * TC_TILE;
-                const int m = warp * 32 + lane;
-                for (int c = 0; c < TC_NB; c += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + ps * TC_NB + c, v);
-#pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const long long g = ts + static_cast<long long>(c + i) * TC_L + m;
-                        if (g < p.n) p.y[g] = v[i];
+                if (D + 2 > 16 && d < 2) {  // D = 16: history columns 16, 17 by lanes 0, 1
+                    for (int i = 0; i < TC_SUB; ++i) {
+                        const int j = grp * TC_SUB + i;
+                        const float v = xhp[j * 2 + d];
+                        const float h = tf32_hi(v);
+                        a2s[swz32(j, D + d)] = h;
+                        a2s[TC_KB + swz32(j, D + d)] = tf32_hi(v - h);
                     }
                 }
+                fence_proxy_async_smem();
+                tc_fence_before();
+                stop = bar_compute_any(*vbail);
+                if (stop) break;
+                if (ct == 0) {
+                    mbar_arrive(&aux->mb_sready);
+                    TC_STAMP(k, 4);
+                }
             }
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
+            // ---- d. tile k-1: outputs ----
+            if (k >= 1) {
+                bool ok = tc_wait(&aux->mb_g2, g2_par & 1u, p.timeout_ns, &aux->bail);
+                if (ok)
+                    ++g2_par;
+                else
+                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                tc_fence_after();
+                if (__all_sync(0xffffffffu, ok)) {
+                    const uint32_t kp = k - 1;
+                    const long long ts = static_cast<long long>(tile_of(kp)) * TC_TILE;
+                    float* patch = scr + cw * 32 * TC_PP;
+#pragma unroll 1
+                    for (int part = 0; part < 2; ++part) {
+                        const int c0 = 32 * hh + 16 * part;
+                        float v[16];
+                        __syncwarp();
+                        tmem_ld16(tacc(kp % 3, c0), v);
+                        float4* prow = reinterpret_cast<float4*>(patch + lane * TC_PP);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) prow[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+                        __syncwarp();
+#pragma unroll
+                        for (int it = 0; it < 4; ++it) {
+                            const int r = it * 8 + (lane >> 2), c4 = lane & 3;
+                            const float4 o = *reinterpret_cast<const float4*>(patch + r * TC_PP + 4 * c4);
+                            const long long g = ts + static_cast<long long>(32 * q + r) * TC_L + c0 + 4 * c4;
+                            if (p.y_vec && g + 3 < p.n) {
+                                *reinterpret_cast<float4*>(p.y + g) = o;
+                            } else {
+                                if (g < p.n) p.y[g] = o.x;
+                                if (g + 1 < p.n) p.y[g + 1] = o.y;
+                                if (g + 2 < p.n) p.y[g + 2] = o.z;
+                                if (g + 3 < p.n) p.y[g + 3] = o.w;
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+                tc_fence_before();
+                if (ct == 0) TC_STAMP(k, 5);
+            }
+            stop = bar_compute_any(*vbail);  // (also: output patches and U share the scratch)
+        }
+        // ---- drain (ct == 0, after the MMA warp has stopped issuing): see below ----
+        if (ct == 0) {
+            for (int s = 0; s < 2; ++s)
+                while (tma_par[s] < tma_real[s] && wait_mbar_bounded(&aux->mb_tma[s], tma_par[s] & 1u, p.timeout_ns))
+                    ++tma_par[s];
         }
         __syncthreads();
-        if (aux->bail) break;
+        // MMAs still in flight end before TMEM is freed (the MMA warp's counts are final now)
+        if (ct == 0) {
+            while (g1_par < aux->g1_issued && wait_mbar_bounded(&aux->mb_g1, g1_par & 1u, p.timeout_ns)) ++g1_par;
+            while (g2_par < aux->g2_issued && wait_mbar_bounded(&aux->mb_g2, g2_par & 1u, p.timeout_ns)) ++g2_par;
+        }
     }
-    // an MMA whose completion wait ran out may still run: wait again (bounded) before freeing
-    if (pend1) (void)wait_mbar_bounded(&aux->mb_g1, ph_g1, p.timeout_ns);
-    if (pend2) (void)wait_mbar_bounded(&aux->mb_g2, ph_g2, p.timeout_ns);
+    if (warp < TC_CW0) __syncthreads();  // pairs with the compute warps' barrier above
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+    if (warp == TC_MW) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
     if (tid == 0) pipe_finish(p.state, epoch);
 }
 
@@ -456,8 +741,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
 // -------------------------------------------------------------------------------------------
 namespace iirhost {
 
+using iirgb::TC_B1KB;
 using iirgb::TC_DMAX;
+using iirgb::TC_H2B;
 using iirgb::TC_KB;
+using iirgb::TC_N1;
+using iirgb::TC_N2;
 using iirgb::TC_L;
 using iirgb::TC_NB;
 using iirgb::TC_TILE;
@@ -465,6 +754,8 @@ using iirgb::TC_TILE;
 struct TcPlan {
     int D = 0, KD = 0, sms = 0, grid_max = 0;
     bool input_normal = false;  // carried states in the input-normal basis (else balanced)
+    int lb_depth = 0;           // truncated lookback depth (0: full decoupled lookback)
+    unsigned long long* prof = nullptr;  // timeline buffer (builds with IIR_PROFILE)
     const void* fn = nullptr;
     float* d_tabs = nullptr;  // a1 image, a2 image, phi, phix, phi_grp, pc, pg (one allocation)
     size_t off_a2 = 0, off_phi = 0, off_phix = 0, off_grp = 0, off_pc = 0, off_pg = 0;
@@ -719,6 +1010,9 @@ void tc_plan_destroy(TcPlan* t) {
 }
 
 IirLaunchState* tc_plan_state(TcPlan* t) { return t ? t->d_state : nullptr; }
+void tc_plan_set_profile(TcPlan* t, unsigned long long* buf) {
+    if (t) t->prof = buf;
+}
 int tc_plan_grid(const TcPlan* t) { return t ? t->grid_max : 0; }
 
 static int tc_alloc_carry(TcPlan* t, size_t tiles) {
@@ -775,34 +1069,55 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
     // ---- state basis: input-normal, else per-section balanced (see state_basis) ----
     t->input_normal = state_basis(secs, K, gain, A1, A2, Phi, Phix);
     // ---- host images (float, swizzled, TF32 hi / lo) and tables ----
-    std::vector<float> img1(static_cast<size_t>(4) * TC_KB, 0.f), img2(static_cast<size_t>(2) * TC_KB, 0.f);
-    for (int m = 0; m < 128; ++m)
+    std::vector<float> img1(static_cast<size_t>(4) * TC_B1KB, 0.f), img2(static_cast<size_t>(2) * TC_H2B, 0.f);
+    for (int m = 0; m < TC_N1; ++m)  // GEMM 1 B operand: rows 0..63 T, 64..79 B (zero beyond D)
         for (int c = 0; c < L; ++c) {
             const float v = static_cast<float>(A1[m * L + c]);
             const float hv = tf32_hi_h(v);
-            const size_t idx = static_cast<size_t>(c >> 5) * TC_KB + swz32h(m, c & 31);
+            const size_t idx = static_cast<size_t>(c >> 5) * TC_B1KB + swz32h(m, c & 31);
             img1[idx] = hv;
-            img1[2 * TC_KB + idx] = tf32_hi_h(v - hv);
+            img1[2 * TC_B1KB + idx] = tf32_hi_h(v - hv);
         }
-    for (int m = 0; m < 128; ++m)
+    for (int m = 0; m < TC_N2; ++m)  // GEMM 2 B operand: rows = outputs, K = [H | Hx]
         for (int c = 0; c < 32; ++c) {
             const float v = static_cast<float>(A2[m * 32 + c]);
             const float hv = tf32_hi_h(v);
             img2[swz32h(m, c)] = hv;
-            img2[TC_KB + swz32h(m, c)] = tf32_hi_h(v - hv);
+            img2[TC_H2B + swz32h(m, c)] = tf32_hi_h(v - hv);
         }
     const int KD = t->KD;
-    std::vector<float> phi(TC_DMAX * TC_DMAX), phix(TC_DMAX * 2), grp(static_cast<size_t>(16) * TC_DMAX * TC_DMAX),
+    std::vector<float> phi(TC_DMAX * TC_DMAX), phix(TC_DMAX * 2), ppow(static_cast<size_t>(4) * TC_DMAX * TC_DMAX),
         pc(static_cast<size_t>(33) * KD * KD), pg(static_cast<size_t>(33) * KD * KD);
     for (size_t i = 0; i < phi.size(); ++i) phi[i] = static_cast<float>(Phi[i]);
     for (size_t i = 0; i < phix.size(); ++i) phix[i] = static_cast<float>(Phix[i]);
-    const Mat Phi8 = matpow(Phi, 8, TC_DMAX);
-    Mat P = identity(TC_DMAX);
-    for (int g = 0; g < 16; ++g) {
-        for (int i = 0; i < TC_DMAX * TC_DMAX; ++i) grp[static_cast<size_t>(g) * TC_DMAX * TC_DMAX + i] = static_cast<float>(P[i]);
-        P = matmul(P, Phi8, TC_DMAX);
+    {
+        Mat P = matpow(Phi, 8, TC_DMAX);  // Phi^(8 * 2^b), stored transposed: [b][e][d] = P[d][e]
+        for (int b = 0; b < 4; ++b) {
+            for (int dd = 0; dd < TC_DMAX; ++dd)
+                for (int e = 0; e < TC_DMAX; ++e)
+                    ppow[(static_cast<size_t>(b) * TC_DMAX + e) * TC_DMAX + dd] = static_cast<float>(P[dd * TC_DMAX + e]);
+            P = matmul(P, P, TC_DMAX);
+        }
     }
     const Mat Q = matpow(Phi, TC_NB, TC_DMAX);        // tile transition
+    {
+        // truncated lookback depth: the least m <= TC_LB_MAX with ||Q^m||_inf <= 1e-10
+        Mat Qm = Q;
+        t->lb_depth = 0;
+        for (int m = 1; m <= iirgb::TC_LB_MAX; ++m) {
+            double nrm = 0.0;
+            for (int i = 0; i < TC_DMAX; ++i) {
+                double r = 0.0;
+                for (int j = 0; j < TC_DMAX; ++j) r += std::fabs(Qm[i * TC_DMAX + j]);
+                nrm = std::max(nrm, r);
+            }
+            if (std::isfinite(nrm) && nrm <= 1e-10) {
+                t->lb_depth = m;
+                break;
+            }
+            Qm = matmul(Qm, Q, TC_DMAX);
+        }
+    }
     const Mat Q32 = matpow(Q, 32, TC_DMAX);
     Mat Pq = identity(TC_DMAX), Pq32 = identity(TC_DMAX);
     for (int l = 0; l <= 32; ++l) {
@@ -826,7 +1141,7 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
     t->off_a2 = put(img2);
     t->off_phi = put(phi);
     t->off_phix = put(phix);
-    t->off_grp = put(grp);
+    t->off_grp = put(ppow);
     t->off_pc = put(pc);
     t->off_pg = put(pg);
     int dev = 0;
@@ -878,11 +1193,12 @@ int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long tim
     q.n = static_cast<long long>(n);
     q.state = t->d_state;
     q.carry = t->d_carry;
-    q.a1img = t->d_tabs;
-    q.a2img = t->d_tabs + t->off_a2;
+    q.b1img = t->d_tabs;
+    q.h2img = t->d_tabs + t->off_a2;
     q.phi = t->d_tabs + t->off_phi;
     q.phix = t->d_tabs + t->off_phix;
-    q.phi_grp = t->d_tabs + t->off_grp;
+    q.phi_pow = t->d_tabs + t->off_grp;
+    q.lb_depth = t->lb_depth;
     q.pc = t->d_tabs + t->off_pc;
     q.pg = t->d_tabs + t->off_pg;
     q.timeout_ns = timeout_ns;
@@ -891,6 +1207,8 @@ int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long tim
     q.carry_cap = static_cast<unsigned int>(t->carry_cap);
     q.D = t->D;
     q.use_tma = encode_chunk_rows_map(&q.tmap_x, x, static_cast<long long>(n)) ? 1 : 0;
+    q.y_vec = (reinterpret_cast<uintptr_t>(y) & 15u) == 0 ? 1 : 0;
+    q.prof = t->prof;
     void* args[] = {&q};
     const int grid = static_cast<int>(std::min<size_t>(tiles, static_cast<size_t>(t->grid_max)));
     return cuda_status(cudaLaunchCooperativeKernel(t->fn, dim3(grid), dim3(iirgb::TC_THREADS), args,

@@ -66,3 +66,18 @@ def test_tc_unaligned_and_repeated(cuda_device):
         y = plan(xt)
     plan.check()
     _check(y.cpu().numpy(), x, sos)
+
+
+def test_tc_slow_decay_full_lookback(cuda_device):
+    """A resonance with pole radius 0.99995: the tile transition Phi^128 keeps 66% of the state
+    over a tile, so the truncated lookback does not apply and tiles are joined by the full
+    two-level decoupled lookback."""
+    r, th = 0.99995, 0.01
+    sos = np.array([[1e-4, 0.0, 0.0, 1.0, -2 * r * np.cos(th), r * r],
+                    [1.0, 0.0, 0.0, 1.0, -1.6, 0.64]])
+    n = 300 * 8192 + 11
+    x = np.random.default_rng(5).uniform(-1, 1, n).astype(np.float32)
+    plan = Plan(sos, "TC", max_n=n)
+    y = plan(torch.from_numpy(x).cuda())
+    plan.check()
+    _check(y.cpu().numpy(), x, sos, rms_tol=1e-4)
