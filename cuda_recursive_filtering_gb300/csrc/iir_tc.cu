@@ -40,21 +40,23 @@ constexpr int TC_NB = 128;                // chunks per tile (GEMM M)
 constexpr int TC_TILE = TC_L * TC_NB;     // samples per tile
 constexpr int TC_LBW = 2;                 // lookback warps (tiles alternate between them)
 constexpr int TC_MW = TC_LBW;             // MMA warp
-constexpr int TC_CW0 = TC_LBW + 1;        // first compute warp
-constexpr int TC_CW = 8;                  // compute warps
-constexpr int TC_CT = 32 * TC_CW;         // compute threads
-constexpr int TC_THREADS = 32 * (TC_CW0 + TC_CW);
+constexpr int TC_CW0 = TC_LBW + 1;        // first front warp; the back warps follow
+constexpr int TC_CW = 8;                  // warps per compute group (front, back)
+constexpr int TC_CT = 32 * TC_CW;         // threads per compute group
+constexpr int TC_THREADS = 32 * (TC_CW0 + 2 * TC_CW);
+constexpr int TC_NACC = 4;                // TMEM accumulators (tiles in flight between GEMM 1 and the outputs)
+constexpr int TC_NS = TC_NACC;            // aggregate / X hand-off slots
+constexpr int TC_NXH = TC_NACC + 1;       // input-history slots
 constexpr int TC_GROUPS = 16;             // scan sub-blocks (half-warps)
 constexpr int TC_SUB = TC_NB / TC_GROUPS;  // chunks per sub-block
 constexpr int TC_DMAX = 16;               // carried states (order <= 16)
 constexpr int TC_N1 = 80;                 // GEMM 1 N: 64 outputs + 16 end states
 constexpr int TC_N2 = 64;                 // GEMM 2 N: 64 outputs
-constexpr int TC_ACC = 80;                // TMEM columns per accumulator (3 accumulators)
+constexpr int TC_ACC = 80;                // TMEM columns per accumulator
 constexpr int TC_KB = 32 * TC_NB;         // floats of one swizzled [128 rows x 32] block
 constexpr int TC_B1KB = 32 * TC_N1;       // floats of one swizzled [80 rows x 32] block
 constexpr int TC_H2B = 32 * TC_N2;        // floats of one swizzled [64 rows x 32] block
 constexpr int TC_UP = 17;                 // padded row of the end-state transpose
-constexpr int TC_PP = 20;                 // padded row of an output patch
 constexpr int TC_LB_MAX = 4;              // deepest truncated lookback (tiles)
 
 struct TcParams {
@@ -68,7 +70,7 @@ struct TcParams {
     const float* h2img;          // GEMM 2 B operand [H | Hx]: [hi, lo] x TC_H2B
     const float* phi;            // 16 x 16 (row-major, zero beyond D)
     const float* phix;           // 16 x 2
-    const float* phi_pow;        // Phi^(8 * 2^b), b < 4, transposed: [b][e][d]
+    const float* phi_pow;        // Phi^(8 * 2^b), b < 4: [b][e / 4][d][e % 4] = P[d][e]
     const float* pc;             // Q^l (l <= 32), KD x KD
     const float* pg;             // Q^(32 l) (l <= 32), KD x KD
     long long timeout_ns;
@@ -83,17 +85,17 @@ struct TcParams {
 };
 
 struct TcAux {
-    unsigned long long mb_tma[2], mb_g1, mb_g2, mb_split, mb_sready, mb_agg[TC_LBW], mb_x[TC_LBW];
+    unsigned long long mb_tma[2], mb_g1, mb_g2, mb_split, mb_sready, mb_accfree, mb_agg[TC_NS], mb_x[TC_NS];
     uint32_t tmem;
     uint32_t epoch;
     int bail;
     uint32_t g1_issued, g2_issued;   // MMA batches committed (by the MMA warp)
     int pad;
-    float agg[TC_LBW][TC_DMAX];      // tile aggregate (zero incoming state) for the lookback warp
-    float X[TC_LBW][TC_DMAX];        // incoming state of the tile, from the lookback warp
-    float Ig0[2][TC_GROUPS][TC_DMAX];  // zero-start incoming state of each sub-block, per tile slot
-    float xh[3][TC_NB][2];           // input history of each chunk, per tile slot
-    float phip[4][TC_DMAX][TC_DMAX];   // Phi^(8 * 2^b), transposed
+    float agg[TC_NS][TC_DMAX];       // tile aggregate (zero incoming state), for the lookback warp
+    float X[TC_NS][TC_DMAX];         // incoming state of the tile, from the lookback warp
+    float Ig0[TC_NACC][TC_GROUPS][TC_DMAX];  // zero-start incoming state of each sub-block, per tile
+    float xh[TC_NXH][TC_NB][2];      // input history of each chunk, per tile
+    alignas(16) float phip[4][TC_DMAX / 4][TC_DMAX][4];  // Phi^(8 * 2^b): [b][e / 4][d][e % 4] = P[d][e]
 };
 
 struct TcSmem {
@@ -102,17 +104,20 @@ struct TcSmem {
     static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target, hi)
     static constexpr size_t XL = XS + 4 * TC_KB * 4;            // 2 k-blocks x TC_KB (lo)
     static constexpr size_t A2S = XL + 2 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
-    static constexpr size_t SCR = A2S + 2 * TC_KB * 4;          // scratch: transposes / output patches
-    static constexpr size_t SCR_BYTES = TC_CW * 32 * TC_PP * 4;
-    static constexpr size_t AUX = SCR + SCR_BYTES;
+    static constexpr size_t SCRF = A2S + 2 * TC_KB * 4;         // front scratch: end-state rows, combine
+    static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS * TC_DMAX) * 4;
+    static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, incoming states
+    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS * TC_DMAX) * 4 > TC_CW * 32 * 8 * 4
+                                             ? (TC_NB * TC_UP + TC_GROUPS * TC_DMAX) * 4
+                                             : TC_CW * 32 * 8 * 4;
+    static constexpr size_t AUX = (SCRB + SCRB_BYTES + 15) / 16 * 16;
     static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
 };
 static_assert(TcSmem::H2 % 1024 == 0 && TcSmem::XS % 1024 == 0 && TcSmem::XL % 1024 == 0 && TcSmem::A2S % 1024 == 0,
               "operand blocks on the 1024-byte swizzle atom");
 static_assert((TC_B1KB * 4) % 1024 == 0 && (TC_H2B * 4) % 1024 == 0, "operand blocks on the swizzle atom");
-static_assert((TC_NB * TC_UP + 2 * TC_GROUPS * TC_DMAX) * 4 <= TcSmem::SCR_BYTES, "scan scratch");
 static_assert(TcSmem::BYTES <= 232448, "shared memory");
-static_assert(3 * TC_ACC <= 256, "TMEM columns");
+static_assert(TC_NACC * TC_ACC <= 512, "TMEM columns");
 
 __device__ __forceinline__ int swz32(int r, int c) { return (r << 5) + ((((c >> 2) ^ (r & 7))) << 2) + (c & 3); }
 // Nearest TF32 value of v (ties away from zero): round the magnitude at mantissa bit 13. The
@@ -151,6 +156,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+        "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
     uint32_t r[8];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -162,15 +181,15 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// barrier of the compute warps only (named barrier 1)
-__device__ __forceinline__ void bar_compute() { asm volatile("bar.sync 1, %0;" ::"r"(TC_CT) : "memory"); }
+// barrier of one compute group (named barrier 1: front, 2: back)
+__device__ __forceinline__ void bar_group(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(TC_CT) : "memory"); }
 
 // Optional timeline (compiled in with -DIIR_PROFILE): per block, per tile iteration k < 16,
-// 8 global-timer stamps.
+// 16 SM-clock stamps.
 #ifdef IIR_PROFILE
 #define TC_STAMP(k, slot)                                                                                 \
     do {                                                                                                  \
-        if (p.prof && (k) < 16u) p.prof[(static_cast<size_t>(blockIdx.x) * 16 + (k)) * 8 + (slot)] = globaltimer_ns(); \
+        if (p.prof && (k) < 16u) p.prof[(static_cast<size_t>(blockIdx.x) * 16 + (k)) * 16 + (slot)] = clock64(); \
     } while (0)
 #else
 #define TC_STAMP(k, slot) \
@@ -178,13 +197,13 @@ __device__ __forceinline__ void bar_compute() { asm volatile("bar.sync 1, %0;" :
     } while (0)
 #endif
 
-// Barrier of the compute warps that also returns, to every one of them, whether any passed `v`.
-__device__ __forceinline__ bool bar_compute_any(bool v) {
+// Barrier of one compute group that also returns, to every one of its threads, whether any passed `v`.
+__device__ __forceinline__ bool bar_group_any(int id, bool v) {
     uint32_t r;
     asm volatile(
-        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
         : "=r"(r)
-        : "r"(static_cast<uint32_t>(v)), "r"(TC_CT)
+        : "r"(static_cast<uint32_t>(v)), "r"(id), "r"(TC_CT)
         : "memory");
     return r != 0u;
 }
@@ -254,16 +273,20 @@ __device__ bool lookback_trunc(const TcParams& p, const unsigned long long* slot
     return true;
 }
 
-// Persistent tile pipeline.
-//   warps 0 .. TC_LBW-1   lookback of alternate tiles (truncated, or the full two-level one)
-//   warp  TC_MW           tcgen05.mma issue (GEMM 1 of a staged tile, GEMM 2 of a solved one)
-//   TC_CW compute warps   per iteration k, on three tiles in flight:
-//     b. tile k:   GEMM 1 done -> end-state rows from TMEM -> sub-block scans -> aggregate -> lookback
-//     a. tile k+1: TMA data landed -> input history, TF32 split -> GEMM 1
-//     c. tile k-1: lookback's X -> states of its chunks -> GEMM 2
-//     d. tile k-1: GEMM 2 done -> outputs from TMEM -> y
-// The lookback of tile k runs while the compute warps do a(k+1) .. b(k+1); TMEM holds three
-// accumulators (tiles k-1, k, k+1); x is double-buffered (TMA two tiles ahead).
+// Persistent tile pipeline, per block:
+//   warps 0 .. TC_LBW-1  lookback of alternate tiles (truncated, or the full two-level one)
+//   warp  TC_MW          tcgen05.mma issue: GEMM 1 of a staged tile once its accumulator is
+//                        free, GEMM 2 of a solved tile
+//   front group (TC_CW warps), per tile k:
+//     b. GEMM 1 done -> end-state rows from TMEM -> sub-block scans -> aggregate -> lookback
+//     a. tile k+1: TMA data landed -> input history, TF32 split -> MMA warp
+//   back group (TC_CW warps), per tile k:
+//     c. lookback's X -> states of the tile's chunks -> MMA warp (GEMM 2)
+//     d. GEMM 2 done -> outputs from TMEM -> y -> accumulator free
+// The groups meet only through mbarriers, so the back group's rescan and stores of one tile run
+// beside the front group's scan and split of later tiles. TMEM holds three accumulators; x is
+// double-buffered (TMA two tiles ahead); the lookback of tile k runs while the front group
+// stages tile k+1 and scans it.
 template <int KD>
 __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_constant__ TcParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -274,7 +297,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     float* xs = reinterpret_cast<float*>(base + TcSmem::XS);
     float* xl = reinterpret_cast<float*>(base + TcSmem::XL);
     float* a2s = reinterpret_cast<float*>(base + TcSmem::A2S);
-    float* scr = reinterpret_cast<float*>(base + TcSmem::SCR);
     TcAux* aux = reinterpret_cast<TcAux*>(base + TcSmem::AUX);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int D = p.D;
@@ -292,12 +314,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         for (int i = tid; i < TC_H2B / 2; i += TC_THREADS) d2[i] = __ldg(s2 + i);  // 2 x TC_H2B floats
         float4* z = reinterpret_cast<float4*>(a2s);
         for (int i = tid; i < TC_KB / 2; i += TC_THREADS) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // 2 x TC_KB
-        float* pp = &aux->phip[0][0][0];
+        float* pp = &aux->phip[0][0][0][0];
         for (int i = tid; i < 4 * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
     }
     if (warp == TC_MW) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&aux->tmem)),
-                     "r"(256));
+                     "r"(512));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
@@ -307,7 +329,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         mbar_init(&aux->mb_g2, 1);
         mbar_init(&aux->mb_split, 1);
         mbar_init(&aux->mb_sready, 1);
-        for (int w = 0; w < TC_LBW; ++w) {
+        mbar_init(&aux->mb_accfree, 1);
+        for (int w = 0; w < TC_NS; ++w) {
             mbar_init(&aux->mb_agg[w], 1);
             mbar_init(&aux->mb_x[w], 1);
         }
@@ -324,26 +347,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     unsigned long long* slots = p.carry;
     unsigned long long* gslots = p.carry + static_cast<size_t>(p.carry_cap) * 2 * KD;
     volatile int* vbail = &aux->bail;
+    auto tile_of = [&](uint32_t kk) { return blockIdx.x + kk * G; };
 
     if (warp < TC_LBW) {
         // ================= lookback warps: tiles k = warp, warp + TC_LBW, ... =================
         const uint32_t ff = 2u * epoch + 2u;
         for (uint32_t k = warp; k < nk; k += TC_LBW) {
-            const uint32_t par = (k / TC_LBW) & 1u;
+            const int sl = k % TC_NS;
             int got = 0;
             if (lane == 0) {
-                got = tc_wait(&aux->mb_agg[warp], par, wait_lim, &aux->bail) ? 1 : 0;
+                got = tc_wait(&aux->mb_agg[sl], (k / TC_NS) & 1u, wait_lim, &aux->bail) ? 1 : 0;
                 if (!got) tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
                 else if (*vbail) got = 0;
             }
             __syncwarp();
             if (!__shfl_sync(FULL_MASK, got, 0)) break;
-            const uint32_t t = blockIdx.x + k * G;
-            if (lane == 0) TC_STAMP(k, 6);
+            const uint32_t t = tile_of(k);
+            if (lane == 0) TC_STAMP(k, 13);
             float own[KD], X[KD];
 #pragma unroll
             for (int e = 0; e < KD; ++e) {
-                own[e] = aux->agg[warp][e];
+                own[e] = aux->agg[sl][e];
                 X[e] = 0.f;
             }
             const bool withhold = static_cast<long long>(t) == p.withhold_chunk;
@@ -364,75 +388,96 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 }
                 if (!ok) atomicExch(&aux->bail, 1);  // the lookback has reported its timeout
 #pragma unroll
-                for (int e = 0; e < TC_DMAX; ++e) aux->X[warp][e] = e < KD ? X[e] : 0.f;
-                mbar_arrive(&aux->mb_x[warp]);
-                TC_STAMP(k, 7);
+                for (int e = 0; e < TC_DMAX; ++e) aux->X[sl][e] = e < KD ? X[e] : 0.f;
+                mbar_arrive(&aux->mb_x[sl]);
+                TC_STAMP(k, 14);
             }
             __syncwarp();
             if (!ok) break;
         }
     } else if (warp == TC_MW) {
-        // ================= MMA warp: the compute warps' order, a(k+1) then c(k-1) =================
+        // ===== MMA warp: GEMM 2 of a solved tile first (the back group waits on it), GEMM 1 of
+        // a staged tile in four pieces of six MMAs so a ready GEMM 2 never queues behind a whole
+        // GEMM 1. GEMM 1 of tile k also needs accumulator k % TC_NACC back from tile k - TC_NACC. =====
+        // Every barrier phase is observed in order and at most one completed phase of each is
+        // unobserved: split(k + 1) needs GEMM 1 of tile k done, sready(k + 1) and accfree(k + 1)
+        // need GEMM 2 of tile k, which is issued only after accfree(k - 1) was observed.
         if (lane == 0) {
-            uint32_t n_split = 0, n_sready = 0;
-            auto gemm1 = [&](uint32_t kk) {
-                if (!tc_wait(&aux->mb_split, n_split & 1u, wait_lim, &aux->bail)) return false;
-                ++n_split;
-                tc_fence_after();
-                const float* xt = xs + (kk & 1) * 2 * TC_KB;
-                const uint32_t dt = tmem + static_cast<uint32_t>((kk % 3) * TC_ACC);
-                uint32_t acc = 0;
-#pragma unroll
-                for (int kb = 0; kb < 2; ++kb) {
+            uint32_t k1 = 0, k2 = 0, piece = 0, n_free = 0;
+            bool got_split = false;
+            uint64_t t_last = globaltimer_ns();
+            uint32_t spins = 0;
+            while (k1 < nk || k2 < nk) {
+                bool progress = false;
+                if (n_free < k2 && mbar_try_wait(&aux->mb_accfree, n_free & 1u)) {
+                    ++n_free;
+                    progress = true;
+                }
+                if (k2 < k1 && n_free >= k2 && mbar_try_wait(&aux->mb_sready, k2 & 1u)) {
+                    tc_fence_after();
+                    const uint32_t dt = tmem + static_cast<uint32_t>((k2 % TC_NACC) * TC_ACC);
 #pragma unroll
                     for (int ks = 0; ks < 4; ++ks) {
-                        const uint32_t oa = (kb * TC_KB) * 4 + ks * 32;
-                        const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
-                        const uint64_t ah = umma_desc(smem_u32(xt) + oa);
-                        const uint64_t al = umma_desc(smem_u32(xl) + oa);
-                        const uint64_t bh = umma_desc(smem_u32(b1) + ob);
-                        const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
-                        umma_tf32(dt, ah, bh, TC_IDESC1, acc);
-                        umma_tf32(dt, ah, bl, TC_IDESC1, 1u);
-                        umma_tf32(dt, al, bh, TC_IDESC1, 1u);
-                        acc = 1u;
+                        const uint32_t o = ks * 32;
+                        const uint64_t ah = umma_desc(smem_u32(a2s) + o);
+                        const uint64_t al = umma_desc(smem_u32(a2s) + TC_KB * 4 + o);
+                        const uint64_t bh = umma_desc(smem_u32(h2) + o);
+                        const uint64_t bl = umma_desc(smem_u32(h2) + TC_H2B * 4 + o);
+                        umma_tf32(dt, ah, bh, TC_IDESC2, 1u);
+                        umma_tf32(dt, ah, bl, TC_IDESC2, 1u);
+                        umma_tf32(dt, al, bh, TC_IDESC2, 1u);
+                    }
+                    umma_commit(&aux->mb_g2);
+                    ++aux->g2_issued;
+                    ++k2;
+                    progress = true;
+                } else if (k1 < nk && (k1 < TC_NACC || n_free + TC_NACC > k1)) {  // accumulator k1 % TC_NACC is free
+                    if (!got_split) got_split = mbar_try_wait(&aux->mb_split, k1 & 1u);
+                    if (got_split) {
+                        if (piece == 0) tc_fence_after();
+                        const float* xt = xs + (k1 & 1) * 2 * TC_KB;
+                        const uint32_t dt = tmem + static_cast<uint32_t>((k1 % TC_NACC) * TC_ACC);
+                        const int kb = piece >> 1;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const int ks = (piece & 1) * 2 + h;
+                            const uint32_t oa = (kb * TC_KB) * 4 + ks * 32;
+                            const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
+                            const uint64_t ah = umma_desc(smem_u32(xt) + oa);
+                            const uint64_t al = umma_desc(smem_u32(xl) + oa);
+                            const uint64_t bh = umma_desc(smem_u32(b1) + ob);
+                            const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
+                            umma_tf32(dt, ah, bh, TC_IDESC1, (piece == 0 && h == 0) ? 0u : 1u);
+                            umma_tf32(dt, ah, bl, TC_IDESC1, 1u);
+                            umma_tf32(dt, al, bh, TC_IDESC1, 1u);
+                        }
+                        if (++piece == 4) {
+                            umma_commit(&aux->mb_g1);
+                            ++aux->g1_issued;
+                            TC_STAMP(k1, 15);
+                            ++k1;
+                            piece = 0;
+                            got_split = false;
+                        }
+                        progress = true;
                     }
                 }
-                umma_commit(&aux->mb_g1);
-                ++aux->g1_issued;
-                return true;
-            };
-            auto gemm2 = [&](uint32_t kk) {
-                if (!tc_wait(&aux->mb_sready, n_sready & 1u, wait_lim, &aux->bail)) return false;
-                ++n_sready;
-                tc_fence_after();
-                const uint32_t dt = tmem + static_cast<uint32_t>((kk % 3) * TC_ACC);
-#pragma unroll
-                for (int ks = 0; ks < 4; ++ks) {
-                    const uint32_t o = ks * 32;
-                    const uint64_t ah = umma_desc(smem_u32(a2s) + o);
-                    const uint64_t al = umma_desc(smem_u32(a2s) + TC_KB * 4 + o);
-                    const uint64_t bh = umma_desc(smem_u32(h2) + o);
-                    const uint64_t bl = umma_desc(smem_u32(h2) + TC_H2B * 4 + o);
-                    umma_tf32(dt, ah, bh, TC_IDESC2, 1u);
-                    umma_tf32(dt, ah, bl, TC_IDESC2, 1u);
-                    umma_tf32(dt, al, bh, TC_IDESC2, 1u);
+                if (progress) {
+                    t_last = globaltimer_ns();
+                } else if ((++spins & 63u) == 0u) {
+                    if (*vbail) break;
+                    if (globaltimer_ns() - t_last > static_cast<uint64_t>(wait_lim)) {
+                        tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                        break;
+                    }
                 }
-                umma_commit(&aux->mb_g2);
-                ++aux->g2_issued;
-                return true;
-            };
-            bool go = nk == 0 || gemm1(0);
-            for (uint32_t k = 0; go && k <= nk; ++k) {
-                if (k + 1 < nk) go = gemm1(k + 1);
-                if (go && k >= 1) go = gemm2(k - 1);
             }
         }
         __syncwarp();
-    } else {
-        // ================= compute warps =================
-        const int ct = tid - 32 * TC_CW0;       // 0 .. TC_CT-1
-        const int cw = warp - TC_CW0;           // 0 .. TC_CW-1
+    } else if (warp < TC_CW0 + TC_CW) {
+        // ================= front group =================
+        const int ct = tid - 32 * TC_CW0;
+        const int cw = warp - TC_CW0;
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int hh = cw >> 2;                 // which of the two warps on the quadrant
         const int grp = ct >> 4, d = ct & 15;   // scan: sub-block, state component
@@ -441,15 +486,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
         phix0 = __ldg(p.phix + d * 2);
         phix1 = __ldg(p.phix + d * 2 + 1);
-        float* U = scr;                                   // [128][TC_UP] end-state rows
-        float* V0 = scr + TC_NB * TC_UP;                  // [16][16] x 2 combine ping-pong
+        float* U = reinterpret_cast<float*>(base + TcSmem::SCRF);  // [128][TC_UP] end-state rows
+        float* V0 = U + TC_NB * TC_UP;                             // [16][16] x 2 combine ping-pong
         float* V1 = V0 + TC_GROUPS * TC_DMAX;
-        // Waits count completed phases (every compute thread waits on every phase); ct == 0
-        // issues the TMA loads and counts them, for the drain at the end.
-        uint32_t tma_par[2] = {0u, 0u}, g1_par = 0, g2_par = 0;
-        uint32_t tma_real[2] = {0u, 0u};
+        float* SB = V1 + TC_GROUPS * TC_DMAX;                      // [16][16] scan state broadcast
+        uint32_t tma_par[2] = {0u, 0u}, tma_real[2] = {0u, 0u}, g1_par = 0;
 
-        auto tile_of = [&](uint32_t kk) { return blockIdx.x + kk * G; };
         auto bulk = [&](uint32_t kk) {
             return p.use_tma && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
         };
@@ -461,46 +503,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             tma_load_2d(dst + TC_KB, &p.tmap_x, 32, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[s]);
             ++tma_real[s];
         };
-        // TMEM address of accumulator slot s, this warp's lane quadrant, column c
-        auto tacc = [&](int s, int c) {
-            return tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(s * TC_ACC + c);
-        };
-        // end-state rows of tile kk (TMEM columns 64 ..) -> U[chunk][state]
-        auto load_z = [&](uint32_t kk) {
-            float v[8];
+        // one recurrence step of the half-warp's state, Phi S + Z_j + Phix xh_j; the state goes
+        // through the group's 16-float buffer sb (one store, four broadcast vector loads)
+        auto step = [&](float S, int j, const float* xhj, float* sb) {
             __syncwarp();
-            tmem_ld8(tacc(kk % 3, 64 + 8 * hh), v);
-            float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) u[i] = v[i];
-        };
-        // one recurrence step of the half-warp's state: Phi S + Z_j + Phix xh_j
-        auto step = [&](float S, int j, const float* xhj) {
+            sb[d] = S;
+            __syncwarp();
+            const float4* s4 = reinterpret_cast<const float4*>(sb);
             float s0 = U[j * TC_UP + d], s1 = phix0 * xhj[0], s2 = phix1 * xhj[1], s3 = 0.f;
 #pragma unroll
             for (int e = 0; e < KD; e += 4) {
-                s0 = fmaf(phi_row[e], __shfl_sync(0xffffffffu, S, e, 16), s0);
-                if (e + 1 < KD) s1 = fmaf(phi_row[e + 1], __shfl_sync(0xffffffffu, S, e + 1, 16), s1);
-                if (e + 2 < KD) s2 = fmaf(phi_row[e + 2], __shfl_sync(0xffffffffu, S, e + 2, 16), s2);
-                if (e + 3 < KD) s3 = fmaf(phi_row[e + 3], __shfl_sync(0xffffffffu, S, e + 3, 16), s3);
+                const float4 v = s4[e >> 2];
+                s0 = fmaf(phi_row[e], v.x, s0);
+                if (e + 1 < KD) s1 = fmaf(phi_row[e + 1], v.y, s1);
+                if (e + 2 < KD) s2 = fmaf(phi_row[e + 2], v.z, s2);
+                if (e + 3 < KD) s3 = fmaf(phi_row[e + 3], v.w, s3);
             }
             return (s0 + s1) + (s2 + s3);
         };
-        // y_d = sum_e M[d][e] v_e with M = Phi^(8 * 2^b) (transposed in shared memory), v a
-        // vector in shared memory
-        auto mv_smem = [&](int b, const float* v) {
-            const float* mt = &aux->phip[b][0][0];
-            float s0 = 0.f, s1 = 0.f;
+        auto mv_smem = [&](int b, const float* v) {  // (Phi^(8 * 2^b) v)_d, v a 16-byte aligned smem vector
+            const float4* m4 = reinterpret_cast<const float4*>(&aux->phip[b][0][d][0]);
+            const float4* v4 = reinterpret_cast<const float4*>(v);
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
-            for (int e = 0; e < KD; e += 2) {
-                s0 = fmaf(mt[e * TC_DMAX + d], v[e], s0);
-                if (e + 1 < KD) s1 = fmaf(mt[(e + 1) * TC_DMAX + d], v[e + 1], s1);
+            for (int e = 0; e < KD; e += 4) {
+                const float4 mm = m4[(e >> 2) * TC_DMAX], vv = v4[e >> 2];
+                s0 = fmaf(mm.x, vv.x, s0);
+                if (e + 1 < KD) s1 = fmaf(mm.y, vv.y, s1);
+                if (e + 2 < KD) s2 = fmaf(mm.z, vv.z, s2);
+                if (e + 3 < KD) s3 = fmaf(mm.w, vv.w, s3);
             }
-            return s0 + s1;
+            return (s0 + s1) + (s2 + s3);
         };
-        // stage tile kk: data landed (TMA) or gathered, input history, TF32 split, then hand
-        // it to the MMA warp. Returns the block's stop decision (the same in every compute thread).
-        auto stage_tile = [&](uint32_t kk) {
+        // stage tile kk: data landed (TMA) or gathered, input history, TF32 split, then hand it
+        // to the MMA warp. Returns the group's stop decision (the same in all of its threads).
+        auto stage_tile = [&](uint32_t kk, float hx2, float hx1) {
             const int s = kk & 1;
             float* xt = xs + s * 2 * TC_KB;
             const long long ts = static_cast<long long>(tile_of(kk)) * TC_TILE;
@@ -509,29 +546,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                     ++tma_par[s];
                 else
                     tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+                if (ct == 0 && kk > 0) TC_STAMP(kk - 1, 6);
             } else {
                 for (int i = ct; i < TC_TILE; i += TC_CT) {
                     const int j = i / TC_L, c = i % TC_L;
                     const long long g = ts + i;
                     xt[(c >> 5) * TC_KB + swz32(j, c & 31)] = (g < p.n) ? p.x[g] : 0.f;
                 }
-                bar_compute();
+                bar_group(1);
             }
             if (ct < TC_NB) {  // the two samples before each chunk
                 float x2, x1;
                 if (ct > 0) {
                     x2 = xt[TC_KB + swz32(ct - 1, 30)];
                     x1 = xt[TC_KB + swz32(ct - 1, 31)];
-                } else if (ts > 0) {
-                    x2 = p.x[ts - 2];
-                    x1 = p.x[ts - 1];
                 } else {
-                    x2 = x1 = 0.f;
+                    x2 = hx2;  // the two samples before the tile, loaded ahead by the caller
+                    x1 = hx1;
                 }
-                aux->xh[kk % 3][ct][0] = x2;
-                aux->xh[kk % 3][ct][1] = x1;
+                aux->xh[kk % TC_NXH][ct][0] = x2;
+                aux->xh[kk % TC_NXH][ct][1] = x1;
             }
-            bar_compute();
+            bar_group(1);
             float4* h4 = reinterpret_cast<float4*>(xt);
             float4* l4 = reinterpret_cast<float4*>(xl);
             for (int i = ct; i < TC_KB / 2; i += TC_CT) {  // 2 k-blocks x TC_KB floats
@@ -549,188 +585,267 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 l4[i] = l;
             }
             fence_proxy_async_smem();
-            tc_fence_before();
-            const bool stop = bar_compute_any(*vbail);
+            const bool stop = bar_group_any(1, *vbail);
             if (!stop && ct == 0) mbar_arrive(&aux->mb_split);
             return stop;
         };
 
-        // prologue: data of the first two tiles, tile 0 staged
         if (ct == 0) {
             for (uint32_t kk = 0; kk < 2 && kk < nk; ++kk)
                 if (bulk(kk)) issue_tma(kk);
         }
-        bool stop = nk > 0 ? stage_tile(0) : false;
-
-        for (uint32_t k = 0; k <= nk && !stop; ++k) {
+        // the two input samples before tile kk (zero before the signal); loaded one iteration
+        // ahead so the load's latency is not on the staging path
+        auto hist = [&](uint32_t kk, float& h2v, float& h1v) {
+            const long long ts = static_cast<long long>(tile_of(kk)) * TC_TILE;
+            h2v = (ct == 0 && ts > 0 && ts - 2 < p.n) ? p.x[ts - 2] : 0.f;
+            h1v = (ct == 0 && ts > 0 && ts - 1 < p.n) ? p.x[ts - 1] : 0.f;
+        };
+        float hx2 = 0.f, hx1 = 0.f;
+        if (nk > 0) hist(0, hx2, hx1);
+        bool stop = nk > 0 ? stage_tile(0, hx2, hx1) : false;
+        for (uint32_t k = 0; k < nk && !stop; ++k) {
             if (ct == 0) TC_STAMP(k, 0);
+            if (k + 1 < nk) hist(k + 1, hx2, hx1);
             // ---- b. tile k: sub-block scans, tile aggregate, hand-off to the lookback warp ----
-            if (k < nk) {
-                if (tc_wait(&aux->mb_g1, g1_par & 1u, p.timeout_ns, &aux->bail))
-                    ++g1_par;
-                else
-                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
-                tc_fence_after();
-                if (ct == 0 && k + 2 < nk && bulk(k + 2) && !*vbail) issue_tma(k + 2);  // its stage is free
-                load_z(k);
-                if (bar_compute_any(*vbail)) break;
-                const float* xhk = &aux->xh[k % 3][0][0];
-                float S = 0.f;
-                for (int i = 0; i < TC_SUB; ++i) S = step(S, grp * TC_SUB + i, xhk + (grp * TC_SUB + i) * 2);
-                V0[grp * TC_DMAX + d] = S;
-                bar_compute();
-                // inclusive scan over the sub-blocks: V_g += Phi^(8 s) V_(g-s), s = 1, 2, 4, 8
-                float* Vc = V0;
-                float* Vn = V1;
-#pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    const int s = 1 << l;
-                    float a = Vc[grp * TC_DMAX + d];
-                    if (grp >= s) a += mv_smem(l, Vc + (grp - s) * TC_DMAX);
-                    Vn[grp * TC_DMAX + d] = a;
-                    bar_compute();
-                    float* tsw = Vc;
-                    Vc = Vn;
-                    Vn = tsw;
-                }
-                aux->Ig0[k & 1][grp][d] = grp > 0 ? Vc[(grp - 1) * TC_DMAX + d] : 0.f;
-                if (grp == TC_GROUPS - 1) aux->agg[k % TC_LBW][d] = Vc[grp * TC_DMAX + d];
-                bar_compute();
-                if (ct == 0) {
-                    const uint32_t t = tile_of(k);
-                    if (static_cast<long long>(t) != p.withhold_chunk) {
-                        float a[KD];
-#pragma unroll
-                        for (int e = 0; e < KD; ++e) a[e] = aux->agg[k % TC_LBW][e];
-                        publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD, 2u * epoch + 1u, a);
-                    }
-                    mbar_arrive(&aux->mb_agg[k % TC_LBW]);
-                    TC_STAMP(k, 1);
-                }
-            }
-            // ---- a. tile k+1: stage (GEMM 1 of tile k has read the lo buffer) ----
-            if (k + 1 < nk) {
-                stop = stage_tile(k + 1);
-                if (stop) break;
-            }
-            if (ct == 0) TC_STAMP(k, 2);
-            // ---- c. tile k-1: states of its chunks, then GEMM 2 ----
-            if (k >= 1) {
-                const uint32_t kp = k - 1, sl = kp % TC_LBW;
-                if (!tc_wait(&aux->mb_x[sl], (kp / TC_LBW) & 1u, wait_lim, &aux->bail))
-                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
-                if (ct == 0) TC_STAMP(k, 3);
-                load_z(kp);
-                // incoming state of the sub-block: Ig0 + Phi^(8 grp) X, Phi^(8 grp) as a product of
-                // Phi^(8 * 2^b) over the bits of grp (the vector goes through the scratch V0)
-                float* vx = V0 + grp * TC_DMAX;
-                vx[d] = aux->X[sl][d];
+            if (tc_wait(&aux->mb_g1, g1_par & 1u, wait_lim, &aux->bail))
+                ++g1_par;
+            else
+                tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+            tc_fence_after();
+            if (ct == 0) TC_STAMP(k, 1);
+            if (ct == 0 && k + 2 < nk && bulk(k + 2) && !*vbail) issue_tma(k + 2);  // its stage is free
+            {
+                float v[8];
                 __syncwarp();
+                tmem_ld8(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((k % TC_NACC) * TC_ACC + 64 + 8 * hh), v);
+                float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
 #pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const float w = mv_smem(b, vx);
-                    __syncwarp();
-                    if ((grp >> b) & 1) vx[d] = w;
-                    __syncwarp();
-                }
-                const float xin = vx[d];
-                if (bar_compute_any(*vbail)) break;
-                const float* xhp = &aux->xh[kp % 3][0][0];
-                float S = aux->Ig0[kp & 1][grp][d] + xin;
-                for (int i = 0; i < TC_SUB; ++i) {
-                    const int j = grp * TC_SUB + i;
-                    if (d < D) {
-                        const float h = tf32_hi(S);
-                        a2s[swz32(j, d)] = h;
-                        a2s[TC_KB + swz32(j, d)] = tf32_hi(S - h);
-                    } else if (d < D + 2) {  // the chunk's input history in columns D, D + 1
-                        const float v = xhp[j * 2 + (d - D)];
-                        const float h = tf32_hi(v);
-                        a2s[swz32(j, d)] = h;
-                        a2s[TC_KB + swz32(j, d)] = tf32_hi(v - h);
-                    }
-                    S = step(S, j, xhp + j * 2);
-                }
-                if (D + 2 > 16 && d < 2) {  // D = 16: history columns 16, 17 by lanes 0, 1
-                    for (int i = 0; i < TC_SUB; ++i) {
-                        const int j = grp * TC_SUB + i;
-                        const float v = xhp[j * 2 + d];
-                        const float h = tf32_hi(v);
-                        a2s[swz32(j, D + d)] = h;
-                        a2s[TC_KB + swz32(j, D + d)] = tf32_hi(v - h);
-                    }
-                }
-                fence_proxy_async_smem();
-                tc_fence_before();
-                stop = bar_compute_any(*vbail);
-                if (stop) break;
-                if (ct == 0) {
-                    mbar_arrive(&aux->mb_sready);
-                    TC_STAMP(k, 4);
-                }
+                for (int i = 0; i < 8; ++i) u[i] = v[i];
             }
-            // ---- d. tile k-1: outputs ----
-            if (k >= 1) {
-                bool ok = tc_wait(&aux->mb_g2, g2_par & 1u, p.timeout_ns, &aux->bail);
-                if (ok)
-                    ++g2_par;
-                else
-                    tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
-                tc_fence_after();
-                if (__all_sync(0xffffffffu, ok)) {
-                    const uint32_t kp = k - 1;
-                    const long long ts = static_cast<long long>(tile_of(kp)) * TC_TILE;
-                    float* patch = scr + cw * 32 * TC_PP;
-#pragma unroll 1
-                    for (int part = 0; part < 2; ++part) {
-                        const int c0 = 32 * hh + 16 * part;
-                        float v[16];
-                        __syncwarp();
-                        tmem_ld16(tacc(kp % 3, c0), v);
-                        float4* prow = reinterpret_cast<float4*>(patch + lane * TC_PP);
-#pragma unroll
-                        for (int i = 0; i < 4; ++i) prow[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-                        __syncwarp();
-#pragma unroll
-                        for (int it = 0; it < 4; ++it) {
-                            const int r = it * 8 + (lane >> 2), c4 = lane & 3;
-                            const float4 o = *reinterpret_cast<const float4*>(patch + r * TC_PP + 4 * c4);
-                            const long long g = ts + static_cast<long long>(32 * q + r) * TC_L + c0 + 4 * c4;
-                            if (p.y_vec && g + 3 < p.n) {
-                                *reinterpret_cast<float4*>(p.y + g) = o;
-                            } else {
-                                if (g < p.n) p.y[g] = o.x;
-                                if (g + 1 < p.n) p.y[g + 1] = o.y;
-                                if (g + 2 < p.n) p.y[g + 2] = o.z;
-                                if (g + 3 < p.n) p.y[g + 3] = o.w;
-                            }
-                        }
-                        __syncwarp();
-                    }
-                }
-                tc_fence_before();
-                if (ct == 0) TC_STAMP(k, 5);
+            if (bar_group_any(1, *vbail)) break;
+            if (ct == 0) TC_STAMP(k, 2);
+            const float* xhk = &aux->xh[k % TC_NXH][0][0];
+            float S = 0.f;
+            for (int i = 0; i < TC_SUB; ++i)
+                S = step(S, grp * TC_SUB + i, xhk + (grp * TC_SUB + i) * 2, SB + grp * TC_DMAX);
+            V0[grp * TC_DMAX + d] = S;
+            if (ct == 0) TC_STAMP(k, 3);
+            // ---- a. tile k+1: stage it now (GEMM 1 of tile k has read the lo buffer), so its
+            // GEMM 1 runs while this tile's sub-block results are combined ----
+            if (k + 1 < nk) {
+                if (stage_tile(k + 1, hx2, hx1)) break;
+            } else {
+                bar_group(1);
             }
-            stop = bar_compute_any(*vbail);  // (also: output patches and U share the scratch)
+            if (ct == 0) TC_STAMP(k, 7);
+            // inclusive scan over the sub-blocks: V_g += Phi^(8 s) V_(g-s), s = 1, 2, 4, 8
+            float* Vc = V0;
+            float* Vn = V1;
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                const int s = 1 << l;
+                float a = Vc[grp * TC_DMAX + d];
+                if (grp >= s) a += mv_smem(l, Vc + (grp - s) * TC_DMAX);
+                Vn[grp * TC_DMAX + d] = a;
+                bar_group(1);
+                float* tsw = Vc;
+                Vc = Vn;
+                Vn = tsw;
+            }
+            if (ct == 0) TC_STAMP(k, 4);
+            aux->Ig0[k % TC_NACC][grp][d] = grp > 0 ? Vc[(grp - 1) * TC_DMAX + d] : 0.f;
+            if (grp == TC_GROUPS - 1) aux->agg[k % TC_NS][d] = Vc[grp * TC_DMAX + d];
+            bar_group(1);
+            if (ct == 0) {
+                const uint32_t t = tile_of(k);
+                if (static_cast<long long>(t) != p.withhold_chunk) {
+                    float a[KD];
+#pragma unroll
+                    for (int e = 0; e < KD; ++e) a[e] = aux->agg[k % TC_NS][e];
+                    publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD, 2u * epoch + 1u, a);
+                }
+                mbar_arrive(&aux->mb_agg[k % TC_NS]);
+                TC_STAMP(k, 5);
+            }
+            stop = bar_group_any(1, *vbail);
         }
-        // ---- drain (ct == 0, after the MMA warp has stopped issuing): see below ----
         if (ct == 0) {
             for (int s = 0; s < 2; ++s)
                 while (tma_par[s] < tma_real[s] && wait_mbar_bounded(&aux->mb_tma[s], tma_par[s] & 1u, p.timeout_ns))
                     ++tma_par[s];
         }
         __syncthreads();
-        // MMAs still in flight end before TMEM is freed (the MMA warp's counts are final now)
-        if (ct == 0) {
+        if (ct == 0)  // GEMM 1 batches still in flight end before TMEM is freed
             while (g1_par < aux->g1_issued && wait_mbar_bounded(&aux->mb_g1, g1_par & 1u, p.timeout_ns)) ++g1_par;
-            while (g2_par < aux->g2_issued && wait_mbar_bounded(&aux->mb_g2, g2_par & 1u, p.timeout_ns)) ++g2_par;
+    } else {
+        // ================= back group =================
+        const int ct = tid - 32 * (TC_CW0 + TC_CW);
+        const int cw = warp - TC_CW0 - TC_CW;
+        const int q = warp & 3;
+        const int hh = cw >> 2;
+        const int grp = ct >> 4, d = ct & 15;
+        float phi_row[KD], phix0, phix1;
+#pragma unroll
+        for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
+        phix0 = __ldg(p.phix + d * 2);
+        phix1 = __ldg(p.phix + d * 2 + 1);
+        float* scr = reinterpret_cast<float*>(base + TcSmem::SCRB);
+        float* U = scr;                                   // [128][TC_UP] end-state rows
+        float* VX = scr + TC_NB * TC_UP;                  // [16][16] incoming-state products
+        uint32_t g2_par = 0;
+        // one recurrence step of the half-warp's state, Phi S + Z_j + Phix xh_j; the state goes
+        // through the group's 16-float buffer sb (one store, four broadcast vector loads)
+        auto step = [&](float S, int j, const float* xhj, float* sb) {
+            __syncwarp();
+            sb[d] = S;
+            __syncwarp();
+            const float4* s4 = reinterpret_cast<const float4*>(sb);
+            float s0 = U[j * TC_UP + d], s1 = phix0 * xhj[0], s2 = phix1 * xhj[1], s3 = 0.f;
+#pragma unroll
+            for (int e = 0; e < KD; e += 4) {
+                const float4 v = s4[e >> 2];
+                s0 = fmaf(phi_row[e], v.x, s0);
+                if (e + 1 < KD) s1 = fmaf(phi_row[e + 1], v.y, s1);
+                if (e + 2 < KD) s2 = fmaf(phi_row[e + 2], v.z, s2);
+                if (e + 3 < KD) s3 = fmaf(phi_row[e + 3], v.w, s3);
+            }
+            return (s0 + s1) + (s2 + s3);
+        };
+        auto mv_smem = [&](int b, const float* v) {  // (Phi^(8 * 2^b) v)_d, v a 16-byte aligned smem vector
+            const float4* m4 = reinterpret_cast<const float4*>(&aux->phip[b][0][d][0]);
+            const float4* v4 = reinterpret_cast<const float4*>(v);
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+            for (int e = 0; e < KD; e += 4) {
+                const float4 mm = m4[(e >> 2) * TC_DMAX], vv = v4[e >> 2];
+                s0 = fmaf(mm.x, vv.x, s0);
+                if (e + 1 < KD) s1 = fmaf(mm.y, vv.y, s1);
+                if (e + 2 < KD) s2 = fmaf(mm.z, vv.z, s2);
+                if (e + 3 < KD) s3 = fmaf(mm.w, vv.w, s3);
+            }
+            return (s0 + s1) + (s2 + s3);
+        };
+        bool stop = false;
+        for (uint32_t k = 0; k < nk && !stop; ++k) {
+            const int sl = k % TC_NS;
+            // ---- c. states of the tile's chunks, then GEMM 2 ----
+            if (!tc_wait(&aux->mb_x[sl], (k / TC_NS) & 1u, wait_lim, &aux->bail))
+                tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+            tc_fence_after();
+            if (ct == 0) TC_STAMP(k, 8);
+            {
+                float v[8];
+                __syncwarp();
+                tmem_ld8(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((k % TC_NACC) * TC_ACC + 64 + 8 * hh), v);
+                float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) u[i] = v[i];
+            }
+            // incoming state of the sub-block: Ig0 + Phi^(8 grp) X, Phi^(8 grp) as a product of
+            // Phi^(8 * 2^b) over the bits of grp
+            float* vx = VX + grp * TC_DMAX;
+            vx[d] = aux->X[sl][d];
+            __syncwarp();
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const float w = mv_smem(b, vx);
+                __syncwarp();
+                if ((grp >> b) & 1) vx[d] = w;
+                __syncwarp();
+            }
+            const float xin = vx[d];
+            if (bar_group_any(2, *vbail)) break;
+            if (ct == 0) TC_STAMP(k, 9);
+            const float* xhp = &aux->xh[k % TC_NXH][0][0];
+            float S = aux->Ig0[k % TC_NACC][grp][d] + xin;
+            for (int i = 0; i < TC_SUB; ++i) {
+                const int j = grp * TC_SUB + i;
+                if (d < D) {
+                    const float h = tf32_hi(S);
+                    a2s[swz32(j, d)] = h;
+                    a2s[TC_KB + swz32(j, d)] = tf32_hi(S - h);
+                } else if (d < D + 2) {  // the chunk's input history in columns D, D + 1
+                    const float v = xhp[j * 2 + (d - D)];
+                    const float h = tf32_hi(v);
+                    a2s[swz32(j, d)] = h;
+                    a2s[TC_KB + swz32(j, d)] = tf32_hi(v - h);
+                }
+                S = step(S, j, xhp + j * 2, vx);
+            }
+            if (D + 2 > 16 && d < 2) {  // D = 16: history columns 16, 17 by lanes 0, 1
+                for (int i = 0; i < TC_SUB; ++i) {
+                    const int j = grp * TC_SUB + i;
+                    const float v = xhp[j * 2 + d];
+                    const float h = tf32_hi(v);
+                    a2s[swz32(j, D + d)] = h;
+                    a2s[TC_KB + swz32(j, D + d)] = tf32_hi(v - h);
+                }
+            }
+            fence_proxy_async_smem();
+            tc_fence_before();
+            if (bar_group_any(2, *vbail)) break;
+            if (ct == 0) {
+                mbar_arrive(&aux->mb_sready);
+                TC_STAMP(k, 10);
+            }
+            // ---- d. outputs ----
+            const bool ok = tc_wait(&aux->mb_g2, g2_par & 1u, wait_lim, &aux->bail);
+            if (ok)
+                ++g2_par;
+            else
+                tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+            tc_fence_after();
+            if (ct == 0) TC_STAMP(k, 11);
+            if (__all_sync(0xffffffffu, ok)) {
+                // this thread's chunk (TMEM lane q*32 + lane) has 32 consecutive outputs in its
+                // registers; they go out through a per-warp patch of 32 chunks x 8 samples in four
+                // rounds, so each store instruction writes 64-byte runs of y (32 B per half row,
+                // half rows swapped every 4 rows: conflict-free writes and reads)
+                const long long ts = static_cast<long long>(tile_of(k)) * TC_TILE;
+                float v[32];
+                __syncwarp();
+                tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((k % TC_NACC) * TC_ACC + 32 * hh), v);
+                float4* patch = reinterpret_cast<float4*>(scr) + cw * 64;  // [32 rows][2 float4]
+                const int sw = (lane >> 2) & 1;
+#pragma unroll
+                for (int part = 0; part < 4; ++part) {
+                    patch[lane * 2 + sw] = make_float4(v[8 * part], v[8 * part + 1], v[8 * part + 2], v[8 * part + 3]);
+                    patch[lane * 2 + (sw ^ 1)] = make_float4(v[8 * part + 4], v[8 * part + 5], v[8 * part + 6], v[8 * part + 7]);
+                    __syncwarp();
+#pragma unroll
+                    for (int it = 0; it < 2; ++it) {
+                        const int r = it * 16 + (lane >> 1), c4 = lane & 1;
+                        const float4 o = patch[r * 2 + (c4 ^ ((r >> 2) & 1))];
+                        const long long g = ts + static_cast<long long>(32 * q + r) * TC_L + 32 * hh + 8 * part + 4 * c4;
+                        if (p.y_vec && g + 3 < p.n) {
+                            *reinterpret_cast<float4*>(p.y + g) = o;
+                        } else {
+                            if (g < p.n) p.y[g] = o.x;
+                            if (g + 1 < p.n) p.y[g + 1] = o.y;
+                            if (g + 2 < p.n) p.y[g + 2] = o.z;
+                            if (g + 3 < p.n) p.y[g + 3] = o.w;
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            tc_fence_before();
+            stop = bar_group_any(2, *vbail);
+            if (!stop && ct == 0) {
+                mbar_arrive(&aux->mb_accfree);
+                TC_STAMP(k, 12);
+            }
         }
+        __syncthreads();
+        if (ct == 0)  // GEMM 2 batches still in flight end before TMEM is freed
+            while (g2_par < aux->g2_issued && wait_mbar_bounded(&aux->mb_g2, g2_par & 1u, p.timeout_ns)) ++g2_par;
     }
-    if (warp < TC_CW0) __syncthreads();  // pairs with the compute warps' barrier above
+    if (warp < TC_CW0) __syncthreads();  // pairs with the compute groups' barrier above
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == TC_MW) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+    if (warp == TC_MW) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
     if (tid == 0) pipe_finish(p.state, epoch);
 }
 
@@ -1091,11 +1206,12 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
     for (size_t i = 0; i < phi.size(); ++i) phi[i] = static_cast<float>(Phi[i]);
     for (size_t i = 0; i < phix.size(); ++i) phix[i] = static_cast<float>(Phix[i]);
     {
-        Mat P = matpow(Phi, 8, TC_DMAX);  // Phi^(8 * 2^b), stored transposed: [b][e][d] = P[d][e]
+        Mat P = matpow(Phi, 8, TC_DMAX);  // Phi^(8 * 2^b), stored [b][e / 4][d][e % 4] = P[d][e]
         for (int b = 0; b < 4; ++b) {
             for (int dd = 0; dd < TC_DMAX; ++dd)
                 for (int e = 0; e < TC_DMAX; ++e)
-                    ppow[(static_cast<size_t>(b) * TC_DMAX + e) * TC_DMAX + dd] = static_cast<float>(P[dd * TC_DMAX + e]);
+                    ppow[((static_cast<size_t>(b) * (TC_DMAX / 4) + e / 4) * TC_DMAX + dd) * 4 + e % 4] =
+                        static_cast<float>(P[dd * TC_DMAX + e]);
             P = matmul(P, P, TC_DMAX);
         }
     }
