@@ -38,15 +38,16 @@ namespace iirgb {
 constexpr int TC_L = 64;                  // samples per chunk (GEMM K)
 constexpr int TC_NB = 128;                // chunks per tile (GEMM M)
 constexpr int TC_TILE = TC_L * TC_NB;     // samples per tile
-constexpr int TC_LBW = 2;                 // lookback warps (tiles alternate between them)
+constexpr int TC_LBW = 1;                 // lookback warps (tiles alternate between them)
 constexpr int TC_MW = TC_LBW;             // MMA warp
 constexpr int TC_CW0 = TC_LBW + 1;        // first front warp; the back warps follow
 constexpr int TC_CW = 8;                  // warps per compute group (front, back)
 constexpr int TC_CT = 32 * TC_CW;         // threads per compute group
 constexpr int TC_THREADS = 32 * (TC_CW0 + 2 * TC_CW);
-constexpr int TC_NACC = 4;                // TMEM accumulators (tiles in flight between GEMM 1 and the outputs)
+constexpr int TC_NACC = 3;                // TMEM accumulators (tiles in flight between GEMM 1 and the outputs)
 constexpr int TC_NS = TC_NACC;            // aggregate / X hand-off slots
-constexpr int TC_NXH = TC_NACC + 1;       // input-history slots
+constexpr int TC_NXH = TC_NACC + 2;       // input-history slots
+constexpr int TC_XCOL = 256;              // TMEM columns of the x operand: 2 buffers x [hi 64 | lo 64]
 constexpr int TC_GROUPS = 16;             // scan sub-blocks (half-warps)
 constexpr int TC_SUB = TC_NB / TC_GROUPS;  // chunks per sub-block
 constexpr int TC_DMAX = 16;               // carried states (order <= 16)
@@ -85,7 +86,7 @@ struct TcParams {
 };
 
 struct TcAux {
-    unsigned long long mb_tma[2], mb_g1, mb_g2, mb_split, mb_sready, mb_accfree, mb_agg[TC_NS], mb_x[TC_NS];
+    unsigned long long mb_tma[2], mb_g1[2], mb_g2, mb_split[2], mb_sready, mb_accfree, mb_agg[TC_NS], mb_x[TC_NS];
     uint32_t tmem;
     uint32_t epoch;
     int bail;
@@ -101,9 +102,8 @@ struct TcAux {
 struct TcSmem {
     static constexpr size_t B1 = 0;                             // 4 x TC_B1KB floats
     static constexpr size_t H2 = B1 + 4 * TC_B1KB * 4;          // 2 x TC_H2B
-    static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target, hi)
-    static constexpr size_t XL = XS + 4 * TC_KB * 4;            // 2 k-blocks x TC_KB (lo)
-    static constexpr size_t A2S = XL + 2 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
+    static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target)
+    static constexpr size_t A2S = XS + 4 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
     static constexpr size_t SCRF = A2S + 2 * TC_KB * 4;         // front scratch: end-state rows, combine
     static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS * TC_DMAX) * 4;
     static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, incoming states
@@ -113,11 +113,11 @@ struct TcSmem {
     static constexpr size_t AUX = (SCRB + SCRB_BYTES + 15) / 16 * 16;
     static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
 };
-static_assert(TcSmem::H2 % 1024 == 0 && TcSmem::XS % 1024 == 0 && TcSmem::XL % 1024 == 0 && TcSmem::A2S % 1024 == 0,
+static_assert(TcSmem::H2 % 1024 == 0 && TcSmem::XS % 1024 == 0 && TcSmem::A2S % 1024 == 0,
               "operand blocks on the 1024-byte swizzle atom");
 static_assert((TC_B1KB * 4) % 1024 == 0 && (TC_H2B * 4) % 1024 == 0, "operand blocks on the swizzle atom");
 static_assert(TcSmem::BYTES <= 232448, "shared memory");
-static_assert(TC_NACC * TC_ACC <= 512, "TMEM columns");
+static_assert(TC_NACC * TC_ACC <= TC_XCOL && TC_XCOL + 256 <= 512, "TMEM columns");
 
 __device__ __forceinline__ int swz32(int r, int c) { return (r << 5) + ((((c >> 2) ^ (r & 7))) << 2) + (c & 3); }
 // Nearest TF32 value of v (ties away from zero): round the magnitude at mantissa bit 13. The
@@ -141,6 +141,23 @@ __device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t da, uint64_t d
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
         "l"(da), "l"(db), "r"(idesc), "r"(acc));
 }
+// A from TMEM (M = 128 lanes, K consecutive 32-bit columns), B from shared memory
+__device__ __forceinline__ void umma_tf32_ta(uint32_t tmem, uint32_t ta, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "r"(ta), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+        "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+        "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void umma_commit(unsigned long long* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
@@ -295,7 +312,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     float* b1 = reinterpret_cast<float*>(base + TcSmem::B1);
     float* h2 = reinterpret_cast<float*>(base + TcSmem::H2);
     float* xs = reinterpret_cast<float*>(base + TcSmem::XS);
-    float* xl = reinterpret_cast<float*>(base + TcSmem::XL);
     float* a2s = reinterpret_cast<float*>(base + TcSmem::A2S);
     TcAux* aux = reinterpret_cast<TcAux*>(base + TcSmem::AUX);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -325,9 +341,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     if (tid == 0) {
         mbar_init(&aux->mb_tma[0], 1);
         mbar_init(&aux->mb_tma[1], 1);
-        mbar_init(&aux->mb_g1, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&aux->mb_g1[b], 1);  // per x buffer: tile k uses buffer k & 1
+            mbar_init(&aux->mb_split[b], 1);
+        }
         mbar_init(&aux->mb_g2, 1);
-        mbar_init(&aux->mb_split, 1);
         mbar_init(&aux->mb_sready, 1);
         mbar_init(&aux->mb_accfree, 1);
         for (int w = 0; w < TC_NS; ++w) {
@@ -400,8 +418,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         // a staged tile in four pieces of six MMAs so a ready GEMM 2 never queues behind a whole
         // GEMM 1. GEMM 1 of tile k also needs accumulator k % TC_NACC back from tile k - TC_NACC. =====
         // Every barrier phase is observed in order and at most one completed phase of each is
-        // unobserved: split(k + 1) needs GEMM 1 of tile k done, sready(k + 1) and accfree(k + 1)
-        // need GEMM 2 of tile k, which is issued only after accfree(k - 1) was observed.
+        // unobserved: split and GEMM 1 barriers are per x buffer (tile k + 2 is staged only after
+        // GEMM 1 of tile k completed), sready(k + 1) and accfree(k + 1) need GEMM 2 of tile k,
+        // which is issued only after accfree(k - 1) was observed.
         if (lane == 0) {
             uint32_t k1 = 0, k2 = 0, piece = 0, n_free = 0;
             bool got_split = false;
@@ -432,27 +451,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                     ++k2;
                     progress = true;
                 } else if (k1 < nk && (k1 < TC_NACC || n_free + TC_NACC > k1)) {  // accumulator k1 % TC_NACC is free
-                    if (!got_split) got_split = mbar_try_wait(&aux->mb_split, k1 & 1u);
+                    if (!got_split) got_split = mbar_try_wait(&aux->mb_split[k1 & 1], (k1 >> 1) & 1u);
                     if (got_split) {
                         if (piece == 0) tc_fence_after();
-                        const float* xt = xs + (k1 & 1) * 2 * TC_KB;
+                        const uint32_t xa = tmem + static_cast<uint32_t>(TC_XCOL + (k1 & 1) * 128);  // x hi; lo at + 64
                         const uint32_t dt = tmem + static_cast<uint32_t>((k1 % TC_NACC) * TC_ACC);
                         const int kb = piece >> 1;
 #pragma unroll
                         for (int h = 0; h < 2; ++h) {
                             const int ks = (piece & 1) * 2 + h;
-                            const uint32_t oa = (kb * TC_KB) * 4 + ks * 32;
+                            const uint32_t ca = static_cast<uint32_t>(kb * 32 + ks * 8);
                             const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
-                            const uint64_t ah = umma_desc(smem_u32(xt) + oa);
-                            const uint64_t al = umma_desc(smem_u32(xl) + oa);
                             const uint64_t bh = umma_desc(smem_u32(b1) + ob);
                             const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
-                            umma_tf32(dt, ah, bh, TC_IDESC1, (piece == 0 && h == 0) ? 0u : 1u);
-                            umma_tf32(dt, ah, bl, TC_IDESC1, 1u);
-                            umma_tf32(dt, al, bh, TC_IDESC1, 1u);
+                            umma_tf32_ta(dt, xa + ca, bh, TC_IDESC1, (piece == 0 && h == 0) ? 0u : 1u);
+                            umma_tf32_ta(dt, xa + ca, bl, TC_IDESC1, 1u);
+                            umma_tf32_ta(dt, xa + 64 + ca, bh, TC_IDESC1, 1u);
                         }
                         if (++piece == 4) {
-                            umma_commit(&aux->mb_g1);
+                            umma_commit(&aux->mb_g1[k1 & 1]);
                             ++aux->g1_issued;
                             TC_STAMP(k1, 15);
                             ++k1;
@@ -568,25 +585,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 aux->xh[kk % TC_NXH][ct][1] = x1;
             }
             bar_group(1);
-            float4* h4 = reinterpret_cast<float4*>(xt);
-            float4* l4 = reinterpret_cast<float4*>(xl);
-            for (int i = ct; i < TC_KB / 2; i += TC_CT) {  // 2 k-blocks x TC_KB floats
-                const float4 v = h4[i];
-                float4 h, l;
-                h.x = tf32_hi(v.x);
-                h.y = tf32_hi(v.y);
-                h.z = tf32_hi(v.z);
-                h.w = tf32_hi(v.w);
-                l.x = tf32_hi(v.x - h.x);
-                l.y = tf32_hi(v.y - h.y);
-                l.z = tf32_hi(v.z - h.z);
-                l.w = tf32_hi(v.w - h.w);
-                h4[i] = h;
-                l4[i] = l;
+            {
+                // this thread's chunk row (TMEM lane 32 q + lane), k-block hh: 32 samples from the
+                // swizzled tile, split hi / lo, stored to the x operand columns of buffer kk & 1
+                const int r = 32 * q + lane;
+                const float4* row = reinterpret_cast<const float4*>(xt + hh * TC_KB + r * 32);
+                const uint32_t xa = tmem + (static_cast<uint32_t>(32 * q) << 16) +
+                                    static_cast<uint32_t>(TC_XCOL + (kk & 1) * 128 + 32 * hh);
+                __syncwarp();
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    float hi[16], lo[16];
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float4 v = row[(4 * half + c) ^ (r & 7)];
+                        hi[4 * c] = tf32_hi(v.x);
+                        hi[4 * c + 1] = tf32_hi(v.y);
+                        hi[4 * c + 2] = tf32_hi(v.z);
+                        hi[4 * c + 3] = tf32_hi(v.w);
+                        lo[4 * c] = tf32_hi(v.x - hi[4 * c]);
+                        lo[4 * c + 1] = tf32_hi(v.y - hi[4 * c + 1]);
+                        lo[4 * c + 2] = tf32_hi(v.z - hi[4 * c + 2]);
+                        lo[4 * c + 3] = tf32_hi(v.w - hi[4 * c + 3]);
+                    }
+                    tmem_st16(xa + 16 * half, hi);
+                    tmem_st16(xa + 64 + 16 * half, lo);
+                }
+                tmem_wait_st();
             }
-            fence_proxy_async_smem();
+            fence_proxy_async_smem();  // the tile's stage is refilled by TMA next
+            tc_fence_before();
             const bool stop = bar_group_any(1, *vbail);
-            if (!stop && ct == 0) mbar_arrive(&aux->mb_split);
+            if (!stop && ct == 0) mbar_arrive(&aux->mb_split[kk & 1]);
             return stop;
         };
 
@@ -604,17 +634,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         float hx2 = 0.f, hx1 = 0.f;
         if (nk > 0) hist(0, hx2, hx1);
         bool stop = nk > 0 ? stage_tile(0, hx2, hx1) : false;
+        if (ct == 0 && 2 < nk && bulk(2) && !stop) issue_tma(2);  // stage 0 was read out
+        if (nk > 1) hist(1, hx2, hx1);
         for (uint32_t k = 0; k < nk && !stop; ++k) {
             if (ct == 0) TC_STAMP(k, 0);
-            if (k + 1 < nk) hist(k + 1, hx2, hx1);
+            // ---- a. tile k+1: staged first (its x buffer was read by GEMM 1 of tile k-1, whose
+            // completion this group saw), so GEMM 1 of tile k runs meanwhile ----
+            if (k + 1 < nk) {
+                if (stage_tile(k + 1, hx2, hx1)) break;
+                if (ct == 0 && k + 3 < nk && bulk(k + 3)) issue_tma(k + 3);  // stage (k+1) & 1 is free
+                if (k + 2 < nk) hist(k + 2, hx2, hx1);
+            }
+            if (ct == 0) TC_STAMP(k, 7);
             // ---- b. tile k: sub-block scans, tile aggregate, hand-off to the lookback warp ----
-            if (tc_wait(&aux->mb_g1, g1_par & 1u, wait_lim, &aux->bail))
+            if (tc_wait(&aux->mb_g1[g1_par & 1], (g1_par >> 1) & 1u, wait_lim, &aux->bail))
                 ++g1_par;
             else
                 tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
             tc_fence_after();
             if (ct == 0) TC_STAMP(k, 1);
-            if (ct == 0 && k + 2 < nk && bulk(k + 2) && !*vbail) issue_tma(k + 2);  // its stage is free
             {
                 float v[8];
                 __syncwarp();
@@ -631,14 +669,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 S = step(S, grp * TC_SUB + i, xhk + (grp * TC_SUB + i) * 2, SB + grp * TC_DMAX);
             V0[grp * TC_DMAX + d] = S;
             if (ct == 0) TC_STAMP(k, 3);
-            // ---- a. tile k+1: stage it now (GEMM 1 of tile k has read the lo buffer), so its
-            // GEMM 1 runs while this tile's sub-block results are combined ----
-            if (k + 1 < nk) {
-                if (stage_tile(k + 1, hx2, hx1)) break;
-            } else {
-                bar_group(1);
-            }
-            if (ct == 0) TC_STAMP(k, 7);
+            bar_group(1);
             // inclusive scan over the sub-blocks: V_g += Phi^(8 s) V_(g-s), s = 1, 2, 4, 8
             float* Vc = V0;
             float* Vn = V1;
@@ -677,7 +708,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         }
         __syncthreads();
         if (ct == 0)  // GEMM 1 batches still in flight end before TMEM is freed
-            while (g1_par < aux->g1_issued && wait_mbar_bounded(&aux->mb_g1, g1_par & 1u, p.timeout_ns)) ++g1_par;
+            while (g1_par < aux->g1_issued &&
+                   wait_mbar_bounded(&aux->mb_g1[g1_par & 1], (g1_par >> 1) & 1u, p.timeout_ns))
+                ++g1_par;
     } else {
         // ================= back group =================
         const int ct = tid - 32 * (TC_CW0 + TC_CW);

@@ -81,3 +81,18 @@ def test_tc_slow_decay_full_lookback(cuda_device):
     y = plan(torch.from_numpy(x).cuda())
     plan.check()
     _check(y.cpu().numpy(), x, sos, rms_tol=1e-4)
+
+
+@pytest.mark.parametrize("order", (2, 16))
+def test_tc_long_signal(order, cuda_device):
+    """2^26 + 12345 samples: about 54 tiles per block, so every hand-off slot, x buffer and
+    accumulator of the tile pipeline is reused many times within one launch."""
+    from scipy import signal
+    sos = signal.butter(order, 0.05, output="sos")
+    n = (1 << 26) + 12345
+    xt = workloads.uniform_signal(n, 7)
+    plan = Plan(sos, "TC", max_n=n)
+    for _ in range(2):
+        y = plan(xt)
+    plan.check()
+    _check(y.cpu().numpy(), xt.cpu().numpy(), sos)
