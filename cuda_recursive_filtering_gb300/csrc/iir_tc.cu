@@ -304,7 +304,9 @@ __device__ bool lookback_trunc(const TcParams& p, const unsigned long long* slot
 // beside the front group's scan and split of later tiles. TMEM holds three accumulators; x is
 // double-buffered (TMA two tiles ahead); the lookback of tile k runs while the front group
 // stages tile k+1 and scans it.
-template <int KD>
+// FULL: the two-level decoupled lookback (tile transitions that have not decayed); otherwise the
+// truncated lookback, and the two-level code is not compiled in (it would raise register use).
+template <int KD, bool FULL>
 __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_constant__ TcParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t a0 = smem_u32(smem_raw);
@@ -390,13 +392,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             const bool withhold = static_cast<long long>(t) == p.withhold_chunk;
             bool ok = true;
-            if (p.lb_depth > 0) {
+            if constexpr (!FULL) {
                 if (t > 0) ok = lookback_trunc<KD>(p, slots, t, epoch, p.lb_depth, X);
             } else if (t > 0) {
                 ok = lookback_hier_k<KD>(p, slots, gslots, p.pc, p.pg, t, epoch, own, withhold, X);
             }
             if (lane == 0) {
-                if (ok && !withhold && p.lb_depth == 0) {
+                if (FULL && ok && !withhold) {
                     float f[KD];
                     matvec<KD>(p.pc + KD * KD, X, f);  // Q X
 #pragma unroll
@@ -1142,8 +1144,9 @@ bool state_basis(const SectionF32* secs, int K, double gain, std::vector<double>
 }
 
 template <int KD>
-const void* tc_kernel_fn() {
-    return reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD>);
+const void* tc_kernel_fn(bool full) {
+    return full ? reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, true>)
+                : reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, false>);
 }
 
 }  // namespace
@@ -1302,7 +1305,11 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
     if (!st) st = cuda_status(cudaMemset(t->d_state, 0, sizeof(IirLaunchState)));
     if (!st) st = tc_alloc_carry(t, (std::max<size_t>(max_n, 1) + TC_TILE - 1) / TC_TILE);
     if (!st) {
-        t->fn = KD == 2 ? tc_kernel_fn<2>() : KD == 4 ? tc_kernel_fn<4>() : KD == 8 ? tc_kernel_fn<8>() : tc_kernel_fn<16>();
+        const bool full = t->lb_depth == 0;
+        t->fn = KD == 2   ? tc_kernel_fn<2>(full)
+                : KD == 4 ? tc_kernel_fn<4>(full)
+                : KD == 8 ? tc_kernel_fn<8>(full)
+                          : tc_kernel_fn<16>(full);
         st = cuda_status(cudaFuncSetAttribute(t->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(iirgb::TcSmem::BYTES)));
     }
