@@ -106,10 +106,8 @@ struct TcSmem {
     static constexpr size_t A2S = XS + 4 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
     static constexpr size_t SCRF = A2S + 2 * TC_KB * 4;         // front scratch: end-state rows, combine
     static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS * TC_DMAX) * 4;
-    static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, incoming states
-    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS * TC_DMAX) * 4 > TC_CW * 32 * 8 * 4
-                                             ? (TC_NB * TC_UP + TC_GROUPS * TC_DMAX) * 4
-                                             : TC_CW * 32 * 8 * 4;
+    static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, states, patches
+    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS * TC_DMAX + TC_CW * 32 * 8) * 4;
     static constexpr size_t AUX = (SCRB + SCRB_BYTES + 15) / 16 * 16;
     static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
 };
@@ -586,8 +584,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 aux->xh[kk % TC_NXH][ct][0] = x2;
                 aux->xh[kk % TC_NXH][ct][1] = x1;
             }
-            bar_group(1);
-            {
+            {  // (the split only reads the staged tile, so it needs no barrier after the capture)
                 // this thread's chunk row (TMEM lane 32 q + lane), k-block hh: 32 samples from the
                 // swizzled tile, split hi / lo, stored to the x operand columns of buffer kk & 1
                 const int r = 32 * q + lane;
@@ -761,25 +758,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             return (s0 + s1) + (s2 + s3);
         };
-        bool stop = false;
-        for (uint32_t k = 0; k < nk && !stop; ++k) {
-            const int sl = k % TC_NS;
-            // ---- c. states of the tile's chunks, then GEMM 2 ----
-            if (!tc_wait(&aux->mb_x[sl], (k / TC_NS) & 1u, wait_lim, &aux->bail))
+        float* vx = VX + grp * TC_DMAX;                  // the group's state buffer
+        float4* patch = reinterpret_cast<float4*>(VX + TC_GROUPS * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
+        float xin = 0.f;
+        // c1. tile kk: the lookback's X, end-state rows from TMEM, Phi^(8 grp) X (a product of
+        // Phi^(8 * 2^b) over the bits of grp); runs while GEMM 2 of the tile before is in flight
+        auto prepare = [&](uint32_t kk) {
+            const int sl = kk % TC_NS;
+            if (!tc_wait(&aux->mb_x[sl], (kk / TC_NS) & 1u, wait_lim, &aux->bail))
                 tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
             tc_fence_after();
-            if (ct == 0) TC_STAMP(k, 8);
-            {
-                float v[8];
-                __syncwarp();
-                tmem_ld8(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((k % TC_NACC) * TC_ACC + 64 + 8 * hh), v);
-                float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
+            if (ct == 0) TC_STAMP(kk, 8);
+            float v[8];
+            __syncwarp();
+            tmem_ld8(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((kk % TC_NACC) * TC_ACC + 64 + 8 * hh), v);
+            float* u = U + (32 * q + lane) * TC_UP + 8 * hh;
 #pragma unroll
-                for (int i = 0; i < 8; ++i) u[i] = v[i];
-            }
-            // incoming state of the sub-block: Ig0 + Phi^(8 grp) X, Phi^(8 grp) as a product of
-            // Phi^(8 * 2^b) over the bits of grp
-            float* vx = VX + grp * TC_DMAX;
+            for (int i = 0; i < 8; ++i) u[i] = v[i];
             vx[d] = aux->X[sl][d];
             __syncwarp();
 #pragma unroll
@@ -789,11 +784,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 if ((grp >> b) & 1) vx[d] = w;
                 __syncwarp();
             }
-            const float xin = vx[d];
-            if (bar_group_any(2, *vbail)) break;
-            if (ct == 0) TC_STAMP(k, 9);
-            const float* xhp = &aux->xh[k % TC_NXH][0][0];
-            float S = aux->Ig0[k % TC_NACC][grp][d] + xin;
+            xin = vx[d];
+        };
+        // c2. tile kk (after a group barrier: its rows are in U, the state operand is free):
+        // states of its chunks into the state operand, then GEMM 2 by the MMA warp
+        auto rescan = [&](uint32_t kk) {
+            if (ct == 0) TC_STAMP(kk, 9);
+            const float* xhp = &aux->xh[kk % TC_NXH][0][0];
+            float S = aux->Ig0[kk % TC_NACC][grp][d] + xin;
             for (int i = 0; i < TC_SUB; ++i) {
                 const int j = grp * TC_SUB + i;
                 if (d < D) {
@@ -819,29 +817,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             fence_proxy_async_smem();
             tc_fence_before();
-            if (bar_group_any(2, *vbail)) break;
-            if (ct == 0) {
+            const bool st = bar_group_any(2, *vbail);
+            if (!st && ct == 0) {
                 mbar_arrive(&aux->mb_sready);
-                TC_STAMP(k, 10);
+                TC_STAMP(kk, 10);
             }
-            // ---- d. outputs ----
+            return st;
+        };
+        // d. tile kk: GEMM 2 done -> outputs. This thread's chunk (TMEM lane 32 q + lane) has 32
+        // consecutive outputs in its registers; they go out through a per-warp patch of 32
+        // chunks x 8 samples in four rounds, so each store instruction writes 64-byte runs of y
+        // (32 B per half row, half rows swapped every 4 rows: conflict-free writes and reads)
+        auto epilogue = [&](uint32_t kk) {
             const bool ok = tc_wait(&aux->mb_g2, g2_par & 1u, wait_lim, &aux->bail);
             if (ok)
                 ++g2_par;
             else
                 tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
             tc_fence_after();
-            if (ct == 0) TC_STAMP(k, 11);
+            if (ct == 0) TC_STAMP(kk, 11);
             if (__all_sync(0xffffffffu, ok)) {
-                // this thread's chunk (TMEM lane q*32 + lane) has 32 consecutive outputs in its
-                // registers; they go out through a per-warp patch of 32 chunks x 8 samples in four
-                // rounds, so each store instruction writes 64-byte runs of y (32 B per half row,
-                // half rows swapped every 4 rows: conflict-free writes and reads)
-                const long long ts = static_cast<long long>(tile_of(k)) * TC_TILE;
+                const long long ts = static_cast<long long>(tile_of(kk)) * TC_TILE;
                 float v[32];
                 __syncwarp();
-                tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((k % TC_NACC) * TC_ACC + 32 * hh), v);
-                float4* patch = reinterpret_cast<float4*>(scr) + cw * 64;  // [32 rows][2 float4]
+                tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((kk % TC_NACC) * TC_ACC + 32 * hh), v);
                 const int sw = (lane >> 2) & 1;
 #pragma unroll
                 for (int part = 0; part < 4; ++part) {
@@ -866,11 +865,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 }
             }
             tc_fence_before();
+        };
+
+        bool stop = false;
+        if (nk > 0) {
+            prepare(0);
+            stop = bar_group_any(2, *vbail) || rescan(0);
+        }
+        for (uint32_t k = 0; k < nk && !stop; ++k) {
+            if (k + 1 < nk) prepare(k + 1);  // overlaps GEMM 2 of tile k
+            epilogue(k);
+            // (also: rows of tile k+1 are in U, and GEMM 2 of tile k has read the state operand)
             stop = bar_group_any(2, *vbail);
-            if (!stop && ct == 0) {
+            if (stop) break;
+            if (ct == 0) {
                 mbar_arrive(&aux->mb_accfree);
                 TC_STAMP(k, 12);
             }
+            if (k + 1 < nk) stop = rescan(k + 1);
         }
         __syncthreads();
         if (ct == 0)  // GEMM 2 batches still in flight end before TMEM is freed
