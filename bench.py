@@ -218,6 +218,41 @@ def run_batching(dev) -> dict:
             "samples": int(off[-1]), "check_rel_max_8_channels": worst}
 
 
+def run_precision(dev, log2n: int) -> dict:
+    """Precision form (kernel TC: the chunk solve as tcgen05 TF32 GEMMs with split products)
+    against the plain PH and STCR_UNROLL realizations on the precision workload: butter(order,
+    0.05) on N(0,1) noise plus 8 tones spanning 60 dB (seed 2), device-resident, CUDA events
+    over 5 launches each; max|err| / RMS(ref) against the FP64 oracle on the first 2^20 outputs."""
+    import torch
+
+    import oracle
+    from cuda_recursive_filtering_gb300 import Plan, workloads
+
+    n = 1 << log2n
+    x = workloads.noise_plus_tones(n, 2, device=dev)
+    y = torch.empty_like(x)
+    head = x[: 1 << 20].cpu().numpy()
+    stream = torch.cuda.current_stream()
+    out = {"workload": f"butter(order, 0.05) SOS on 2^{log2n} samples of N(0,1) noise + 8 tones (60 dB span), "
+                       "seed 2; error = max|err| / RMS(ref) over the first 2^20 outputs"}
+    for order in (8, 16):
+        sos = workloads.butter_sos(order, 0.05)
+        _, ref = oracle.reference_golden(sos, head)
+        row = {}
+        for kname, b, nb in (("TC", 0, 0), ("PH", 32, 64), ("STCR_UNROLL", 32, 64)):
+            pl = Plan(sos, kname, b, nb, max_n=n, device=dev)
+            t = time_plan(pl, x, y, 5, 2, stream)
+            pl.check()
+            e = oracle.errors(y[: 1 << 20].cpu().numpy(), ref)
+            pl.close()
+            row[kname] = {"gsps": round(n / (t * 1e-3) / 1e9, 1), "err": float(f"{e['rel_rms']:.3g}")}
+        row["tc_vs_ph"] = round(row["TC"]["gsps"] / row["PH"]["gsps"], 2)
+        row["tc_vs_stcr_unroll"] = round(row["TC"]["gsps"] / row["STCR_UNROLL"]["gsps"], 2)
+        out[f"order{order}"] = row
+    del x, y
+    return out
+
+
 def run_serving(dev, seconds: float = 2.0) -> dict:
     """Continuous-batching stream server under Poisson arrivals (host chunks in, results back
     on the host): achieved GS/s and request latency percentiles."""
@@ -332,6 +367,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     forms = {}
     if not args.no_forms:
         try:
+            forms["precision"] = run_precision(dev, LOG2N)
+        except Exception as exc:  # report, do not hide
+            forms["precision"] = {"error": str(exc)}
+        try:
             forms["batching"] = run_batching(dev)
         except Exception as exc:  # report, do not hide
             forms["batching"] = {"error": str(exc)}
@@ -374,7 +413,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-sweep", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the batching and serving legs")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision, batching and serving legs")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
