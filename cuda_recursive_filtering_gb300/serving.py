@@ -6,6 +6,8 @@ so chunked output equals whole-stream filtering. A serving step takes the oldest
 every stream that has one and filters them all in one launch (continuous batching: the batch is
 rebuilt every step from whatever has arrived). Host chunks are copied to the device and results
 back on one CUDA stream, so a request is complete when its step's device-to-host copy is.
+A stream's waiting chunks are consecutive pieces of one signal, so a step takes all of them (up to
+``max_stream_samples``) as one segment: a burst on one stream costs one step, not one per chunk.
 Streams and requests are admitted while the device keeps `reserve_bytes` free.
 
 The reference has no serving path: its kernels filter one zero-state signal per launch
@@ -16,6 +18,7 @@ from __future__ import annotations
 
 import collections
 import dataclasses
+import gc
 import time
 
 import numpy as np
@@ -60,7 +63,8 @@ class StreamServer:
     """
 
     def __init__(self, filters, max_batch: int = 1024, max_streams: int = 4096, reserve_bytes: int = 1 << 30,
-                 device=None, keep_outputs: bool = True):
+                 device=None, keep_outputs: bool = True, max_stream_samples: int = 1 << 22,
+                 max_step_samples: int = 1 << 23, step_slots: int = 3):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         with torch.cuda.device(self.device):
             self.batch = Batch(filters, max_segments=max_batch, max_chunks=1 << 16, device=self.device)
@@ -70,13 +74,23 @@ class StreamServer:
             self.states = torch.zeros(2, max_streams, self.width, device=self.device)
         self.max_batch = max_batch
         self.max_streams = max_streams
+        self.max_stream_samples = max_stream_samples  # per stream and step (more chunks wait a step)
+        self.max_step_samples = max_step_samples  # per step: bounds the step's buffers and latency
+        # step buffers, allocated once: pinned host input / output and device input / output of
+        # max_step_samples each, for up to step_slots steps in flight (no allocation while serving)
+        with torch.cuda.device(self.device):
+            self._slots = [{"xh": torch.empty(max_step_samples, pin_memory=True),
+                            "yh": torch.empty(max_step_samples, pin_memory=True),
+                            "xd": torch.empty(max_step_samples, device=self.device),
+                            "yd": torch.empty(max_step_samples, device=self.device), "busy": False}
+                           for _ in range(step_slots)]
         self.keep_outputs = keep_outputs  # copy each request's result out of the step's pinned buffer
         self.reserve = reserve_bytes
         self.streams: dict[int, _Stream] = {}
+        self._sid: dict[int, int] = {}  # id(stream record) -> stream id
         self._free_slots = list(range(max_streams - 1, -1, -1))
         self._next_id = 0
-        self._inflight: collections.deque = collections.deque()  # (event, requests, buffers)
-        self._pinned: list = []  # [capacity, xhost, yhost, busy until its step's results are taken]
+        self._inflight: collections.deque = collections.deque()  # (event, requests, slot, request offsets)
         self._free_bytes, self._free_t = 0, -1.0
         self.completed: list[Request] = []
         self.samples_done = 0
@@ -90,17 +104,6 @@ class StreamServer:
             self._free_t = now
         return self._free_bytes
 
-    def _host_buffers(self, total: int):
-        # pinned input / output buffers for one step, reused once the step that used them is done
-        for entry in self._pinned:
-            if entry[0] >= total and not entry[3]:
-                entry[3] = True
-                return entry
-        cap = 1 << max(16, int(total - 1).bit_length())
-        entry = [cap, torch.empty(cap, pin_memory=True), torch.empty(cap, pin_memory=True), True]
-        self._pinned.append(entry)
-        return entry
-
     def open_stream(self, filter_index: int) -> int:
         if not self._free_slots:
             raise AdmissionError("stream table full")
@@ -111,10 +114,12 @@ class StreamServer:
         slot = self._free_slots.pop()
         self.states[:, slot].zero_()
         self.streams[sid] = _Stream(filter_index, slot)
+        self._sid[id(self.streams[sid])] = sid
         return sid
 
     def close_stream(self, sid: int) -> None:
         s = self.streams.pop(sid)
+        self._sid.pop(id(s), None)
         self._free_slots.append(s.slot)
 
     def state(self, sid: int) -> torch.Tensor:
@@ -126,7 +131,9 @@ class StreamServer:
         """Queues a host chunk (float32) of stream ``sid``; returns its request record."""
         s = self.streams[sid]
         host = np.ascontiguousarray(chunk.numpy() if torch.is_tensor(chunk) else chunk, dtype=np.float32)
-        if self._free() < self.reserve + 8 * host.size:  # device buffers of the step: in + out
+        if host.size > self.max_step_samples:
+            raise AdmissionError("chunk longer than the server's step capacity")
+        if self._free() < self.reserve:
             raise AdmissionError("not enough free device memory for the request")
         req = Request(sid, int(host.size), time.perf_counter() if t_arrival is None else t_arrival)
         s.queue.append((req, host))
@@ -134,40 +141,56 @@ class StreamServer:
 
     # ---------------------------------------------------------------- serving loop
     def step(self) -> int:
-        """One launch over the oldest waiting chunk of every stream that has one (at most
-        ``max_batch``): one host-to-device copy of all of them, one batch launch, one copy of
-        the results back. Returns the number of chunks launched."""
-        picked = []
+        """One launch over every stream that has waiting chunks (at most ``max_batch`` streams):
+        each stream's waiting chunks, concatenated in order, are one segment. One host-to-device
+        copy of all of them, one batch launch, one copy of the results back. Returns the number
+        of requests launched."""
+        picked, reqs, chunks, lens = [], [], [], []
+        total = 0
         for s in self.streams.values():
-            if s.queue:
-                picked.append(s)
-                if len(picked) == self.max_batch:
-                    break
+            if not s.queue:
+                continue
+            if picked and total + s.queue[0][0].samples > self.max_step_samples:
+                break  # the step is full; this stream goes first next time (dict order rotates below)
+            n = 0
+            while s.queue and (n == 0 or (n + s.queue[0][0].samples <= self.max_stream_samples and
+                                          total + n + s.queue[0][0].samples <= self.max_step_samples)):
+                req, host = s.queue.popleft()
+                reqs.append(req)
+                chunks.append(host)
+                n += req.samples
+            picked.append(s)
+            lens.append(n)
+            total += n
+            if len(picked) == self.max_batch:
+                break
         if not picked:
             return 0
-        reqs, chunks = [], []
-        for s in picked:
-            req, host = s.queue.popleft()
-            reqs.append(req)
-            chunks.append(host)
+        if any(s.queue for s in self.streams.values()):
+            # streams left waiting: the picked ones go to the back of the order (round robin)
+            for s in picked:
+                sid = self._sid[id(s)]
+                self.streams[sid] = self.streams.pop(sid)
         k = len(picked)
-        lens = np.fromiter((r.samples for r in reqs), dtype=np.int64, count=k)
+        lens = np.asarray(lens, dtype=np.int64)
         off = np.zeros(k + 1, dtype=np.int64)
         np.cumsum(lens, out=off[1:])
-        total = int(off[-1])
+        req_off = np.zeros(len(reqs) + 1, dtype=np.int64)
+        np.cumsum(np.fromiter((r.samples for r in reqs), dtype=np.int64, count=len(reqs)), out=req_off[1:])
         slots = np.fromiter((s.slot for s in picked), dtype=np.int64, count=k)
         turns = np.fromiter((s.turn for s in picked), dtype=np.int64, count=k)
         filt = np.fromiter((s.filter for s in picked), dtype=np.int32, count=k)
         for s in picked:
             s.turn ^= 1
-        hb = self._host_buffers(max(total, 1))
-        xhost, yhost = hb[1][:max(total, 1)], hb[2][:max(total, 1)]
+        slot = next((sl for sl in self._slots if not sl["busy"]), None)
+        if slot is None:  # every step buffer is in flight: complete the oldest step first
+            self.poll(block=True)
+            slot = next(sl for sl in self._slots if not sl["busy"])
+        slot["busy"] = True
+        xhost, yhost, xin, yout = slot["xh"], slot["yh"], slot["xd"], slot["yd"]
         with torch.cuda.device(self.device), torch.cuda.stream(self.cuda_stream):
-            if total:
-                np.concatenate(chunks, out=xhost.numpy()[:total])
-            xin = torch.empty(max(total, 1), device=self.device)
-            yout = torch.empty_like(xin)
-            xin.copy_(xhost, non_blocking=True)
+            np.concatenate(chunks, out=xhost.numpy()[:total])
+            xin[:total].copy_(xhost[:total], non_blocking=True)
             tab = self.batch.segment_table(k)
             tab["x"][:k] = xin.data_ptr() + 4 * off[:-1]
             tab["y"][:k] = yout.data_ptr() + 4 * off[:-1]
@@ -178,30 +201,29 @@ class StreamServer:
             tab["zi"][:k] = base + row * (turns * self.max_streams + slots)
             tab["zf"][:k] = base + row * ((turns ^ 1) * self.max_streams + slots)
             self.batch.execute_table(tab, k, stream=self.cuda_stream)
-            yhost.copy_(yout, non_blocking=True)
+            yhost[:total].copy_(yout[:total], non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(self.cuda_stream)
-        self._inflight.append((ev, reqs, (xin, yout, hb, off)))
-        return k
+        self._inflight.append((ev, reqs, slot, req_off))
+        return len(reqs)
 
     def poll(self, block: bool = False) -> int:
         """Completes requests whose step has finished; returns how many completed."""
         done = 0
         while self._inflight:
-            ev, reqs, _ = self._inflight[0]
+            ev, reqs, slot, off = self._inflight[0]
             if block:
                 ev.synchronize()
             elif not ev.query():
                 break
             t = time.perf_counter()
-            _, _, hb, off = self._inflight[0][2]
-            yhost = hb[2]
+            yhost = slot["yh"]
             for i, r in enumerate(reqs):
                 r.t_done = t
                 if self.keep_outputs:
                     r.out = yhost[off[i]:off[i + 1]].clone()
                 self.samples_done += r.samples
-            hb[3] = False  # results taken: the step's pinned buffers may be reused
+            slot["busy"] = False  # results taken: the step's buffers may be reused
             self.completed.extend(reqs)
             self._inflight.popleft()
             done += len(reqs)
@@ -229,6 +251,19 @@ def run_poisson_load(server: StreamServer, streams: list[int], rate_sps: float, 
     Returns throughput and latency percentiles."""
     rng = np.random.default_rng(seed)
     pool = rng.standard_normal(1 << 22).astype(np.float32)  # chunk data: slices of one pool
+    # The loop creates tens of thousands of request records a second; a cyclic-GC pass over them
+    # stalls the serving loop for tens of milliseconds, so the collector is paused for the run.
+    gc_was_enabled = gc.isenabled()
+    gc.collect()
+    gc.disable()
+    try:
+        return _poisson_loop(server, streams, rate_sps, duration_s, chunk_lo, chunk_hi, rng, pool, signals)
+    finally:
+        if gc_was_enabled:
+            gc.enable()
+
+
+def _poisson_loop(server, streams, rate_sps, duration_s, chunk_lo, chunk_hi, rng, pool, signals) -> dict:
     mean_chunk = 0.5 * (chunk_lo + chunk_hi)
     rate_req = rate_sps / mean_chunk
     t0 = time.perf_counter()

@@ -50,3 +50,25 @@ def test_poisson_load_reports_latency(cuda_device):
     out = run_poisson_load(srv, streams, rate_sps=2e8, duration_s=0.3, chunk_lo=256, chunk_hi=8192, seed=4)
     assert out["requests"] > 0 and out["samples"] > 0
     assert out["p50_us"] is not None and out["p99_us"] >= out["p50_us"] > 0
+
+
+def test_burst_of_chunks_is_one_segment(cuda_device):
+    """Chunks that queue up on a stream between steps go out in one step as one segment (they
+    are consecutive pieces of the stream's signal); the result equals whole-stream filtering."""
+    filters = _filters()
+    srv = StreamServer(filters, max_batch=16, max_stream_samples=1 << 20)
+    rng = np.random.default_rng(5)
+    sigs, reqs = {}, {}
+    for i in range(6):
+        sid = srv.open_stream(i % len(filters))
+        x = rng.standard_normal(int(rng.integers(20_000, 90_000))).astype(np.float32)
+        cuts = np.sort(rng.choice(np.arange(1, x.size), 11, replace=False))
+        sigs[sid] = x
+        reqs[sid] = [srv.submit(sid, piece) for piece in np.split(x, cuts)]
+    assert srv.step() == sum(len(r) for r in reqs.values())  # every queued chunk in one launch
+    srv.drain()
+    for sid, x in sigs.items():
+        y = np.concatenate([r.out.numpy() for r in reqs[sid]])
+        _, ref = oracle.reference_golden(filters[srv.streams[sid].filter], x)
+        e = oracle.errors(y, ref)
+        assert e["rel_max"] <= 1e-4 and e["rel_rms"] <= 1e-5, (sid, e)
