@@ -68,7 +68,7 @@ def parse_filter_taps(path: str) -> dict:
 
 
 def write_filter_taps(path: str, sos_f32, gain: float, plr_b=None, plr_a=None, cutoff: float = REFERENCE_CUTOFF,
-                      input_fs: float = INPUT_FS, input_freq: float = INPUT_FREQ) -> None:
+                      input_fs: float = INPUT_FS, input_freq: float = INPUT_FREQ, kind: str = "butter") -> None:
     """Writes a header with the same symbols and conventions as the reference's generator."""
     sos_f32 = np.asarray(sos_f32, dtype=np.float32).reshape(-1, 6)
     ns = sos_f32.shape[0]
@@ -76,7 +76,7 @@ def write_filter_taps(path: str, sos_f32, gain: float, plr_b=None, plr_a=None, c
     lines = [
         "// Cascaded-biquad filter taps (b0-normalised float32 sections; FILTER_GAIN must be",
         "// applied to the input). Format of the reference's filter_taps.hpp.",
-        f"// Lowpass, order {2 * ns}, cutoff {cutoff} x Nyquist.",
+        f"// {'Chebyshev type I' if kind == 'cheby1' else 'Butterworth'} lowpass, order {2 * ns}, cutoff {cutoff} x Nyquist.",
         "#pragma once",
         "",
         f"#define FILTER_N_SECTIONS {ns}",
@@ -119,11 +119,116 @@ def normalise_sos(sos) -> tuple[np.ndarray, float]:
     return s.astype(np.float32), gain
 
 
-def design_reference_filter(n_sections: int, cutoff: float = REFERENCE_CUTOFF) -> dict:
-    """The reference's test filter: Butterworth lowpass of order 2K designed in SOS form plus
-    the direct-form taps of the same transfer function for PLR (tools/ref_generate.py:56-81)."""
+def design_reference_filter(n_sections: int, cutoff: float = REFERENCE_CUTOFF, kind: str = "butter",
+                            rp: float = 1.0) -> dict:
+    """The reference's test filter: a lowpass of order 2K designed in SOS form plus the
+    direct-form taps of the same transfer function for PLR (tools/ref_generate.py:56-81).
+    ``kind`` "butter" is the reference's design; "cheby1" (passband ripple ``rp`` dB) follows
+    the same conventions (b0-normalised float32 sections, the removed gain applied to the
+    input, b0-normalised direct-form taps with the recurrence sign y[n] += A[j] y[n-j-1])."""
     from scipy import signal
-    sos = signal.butter(N=2 * n_sections, Wn=cutoff, btype="lowpass", output="sos")
+    if kind == "butter":
+        design = lambda out: signal.butter(N=2 * n_sections, Wn=cutoff, btype="lowpass", output=out)
+    elif kind == "cheby1":
+        design = lambda out: signal.cheby1(N=2 * n_sections, rp=rp, Wn=cutoff, btype="lowpass", output=out)
+    else:
+        raise ValueError(f"unknown filter kind {kind!r} (butter, cheby1)")
+    sos = design("sos")
     sos_f32, gain = normalise_sos(sos)
-    bb, aa = signal.butter(N=2 * n_sections, Wn=cutoff, btype="lowpass", output="ba")
-    return {"sos": sos_f32, "gain": gain, "plr_b": bb[1:] / bb[0], "plr_a": -aa[1:], "sos_f64": sos}
+    bb, aa = design("ba")
+    return {"sos": sos_f32, "gain": gain, "plr_b": bb[1:] / bb[0], "plr_a": -aa[1:], "sos_f64": sos,
+            "kind": kind, "cutoff": cutoff}
+
+
+def generate_reference_files(out_dir: str, n_sections: int, n_samples_log2: int, cutoff: float = REFERENCE_CUTOFF,
+                             kind: str = "butter", rp: float = 1.0) -> dict:
+    """Writes ``reference.bin`` and ``filter_taps.hpp`` into ``out_dir`` the way the reference's
+    generator does (tools/ref_generate.py:56-131): the input is the accuracy test's cosine
+    scaled by the removed gain, the golden output is FP64 sosfilt of the float32 sections and
+    float32 input, and it is cross-checked (relative 1e-4) against the unnormalised design."""
+    import os
+
+    from scipy import signal
+    f = design_reference_filter(n_sections, cutoff, kind, rp)
+    n = 1 << n_samples_log2
+    x = reference_input(n, f["gain"])
+    ref = signal.sosfilt(f["sos"].astype(np.float64), x.astype(np.float64))
+    i = np.arange(n, dtype=np.float64)
+    check = signal.sosfilt(f["sos_f64"], np.cos(2.0 * np.pi * INPUT_FREQ * i / INPUT_FS))
+    rel = float(np.max(np.abs(ref - check)) / max(np.max(np.abs(check)), 1e-30))
+    if rel > 1e-4:
+        raise RuntimeError(f"normalisation cross-check failed: relative {rel:.3e}")
+    os.makedirs(out_dir, exist_ok=True)
+    write_reference_bin(os.path.join(out_dir, "reference.bin"), ref)
+    write_filter_taps(os.path.join(out_dir, "filter_taps.hpp"), f["sos"], f["gain"], f["plr_b"], f["plr_a"],
+                      cutoff=cutoff, kind=kind)
+    return {"n": n, "gain": f["gain"], "cross_check_rel": rel}
+
+
+def check_reference_files(taps_path: str, ref_path: str, kernel: str = "DTCR_UNROLL", block_size: int = 0,
+                          n_blocks: int = 0, device=None) -> dict:
+    """The reference's accuracy driver (src/test_accuracy.cu:116-188) on this library: the
+    input is rebuilt from filter_taps.hpp, filtered on the GPU (``kernel``; "PLR" uses the
+    direct-form taps), and compared with reference.bin by the reference's gate
+    max|err| <= 1e-4 * max|ref|. Returns the errors and the verdict."""
+    import torch
+
+    from .api import Plan, PlrPlan
+    taps = parse_filter_taps(taps_path)
+    ref = read_reference_bin(ref_path).astype(np.float64)
+    n = ref.size
+    x = torch.from_numpy(reference_input(n, taps["gain"], taps["input_fs"], taps["input_freq"]))
+    x = x.to(device if device is not None else "cuda")
+    if kernel.upper() == "PLR":
+        # the direct-form lane: b0-normalised taps, the gain already in the input
+        plan = PlrPlan(taps["plr_b"], taps["plr_a"], 1.0, block_size, n_blocks, max_n=n, device=x.device)
+    else:
+        # the sections are b0-normalised with FILTER_GAIN applied to the input, as in the reference
+        plan = Plan(taps["sos"], kernel, block_size, n_blocks, max_n=n, device=x.device)
+    y = plan(x)
+    plan.check()
+    out = y.cpu().numpy().astype(np.float64)
+    plan.close()
+    err = np.abs(out - ref)
+    finite = bool(np.all(np.isfinite(out)))
+    mref = float(np.max(np.abs(ref))) if n else 0.0
+    max_abs = float(np.max(err)) if (n and finite) else (0.0 if not n else float("inf"))
+    rel_max = max_abs / max(mref, 1e-30)
+    return {"kernel": kernel.upper(), "n": n, "max_abs": max_abs, "rel_max": rel_max, "finite": finite,
+            "pass": finite and rel_max <= 1e-4}
+
+
+def main(argv=None) -> int:
+    """Command line: ``generate`` writes reference.bin and filter_taps.hpp (the reference's
+    generator), ``check`` runs one realization against them (the reference's accuracy driver)."""
+    import argparse
+    import json
+    import os
+    ap = argparse.ArgumentParser(prog="python -m cuda_recursive_filtering_gb300.formats")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    g = sub.add_parser("generate")
+    g.add_argument("--out", required=True)
+    g.add_argument("--n-sections", type=int, required=True)
+    g.add_argument("--n-samples-log2", type=int, default=16)
+    g.add_argument("--cutoff", type=float, default=REFERENCE_CUTOFF)
+    g.add_argument("--kind", default="butter", choices=("butter", "cheby1"))
+    g.add_argument("--rp", type=float, default=1.0)
+    c = sub.add_parser("check")
+    c.add_argument("--dir", required=True, help="folder with reference.bin and filter_taps.hpp")
+    c.add_argument("--kernel", default="DTCR_UNROLL")
+    c.add_argument("--block-size", type=int, default=0)
+    c.add_argument("--n-blocks", type=int, default=0)
+    a = ap.parse_args(argv)
+    if a.cmd == "generate":
+        info = generate_reference_files(a.out, a.n_sections, a.n_samples_log2, a.cutoff, a.kind, a.rp)
+        print(json.dumps(info))
+        return 0
+    res = check_reference_files(os.path.join(a.dir, "filter_taps.hpp"), os.path.join(a.dir, "reference.bin"),
+                                a.kernel, a.block_size, a.n_blocks)
+    print(json.dumps(res))
+    return 0 if res["pass"] else 1
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
+

@@ -99,3 +99,22 @@ def test_workload_generators_are_seeded():
     sos, x = workloads.plain_order2_small(device="cpu")
     g = np.load(os.path.join(GOLDEN, "sosfilt_order2_uniform.npz"))
     assert np.array_equal(sos, g["sos"]) and np.array_equal(x.numpy()[: g["x"].size], g["x"])
+
+
+@pytest.mark.parametrize("kind", ("butter", "cheby1"))
+def test_generate_reference_files(kind, tmp_path):
+    """generate_reference_files writes the reference generator's pair of files: the parsed taps
+    reproduce the design, and reference.bin is FP64 sosfilt of the float32 sections and the
+    float32 input (tools/ref_generate.py:56-131)."""
+    from scipy import signal
+    info = formats.generate_reference_files(str(tmp_path), 4, 12, cutoff=0.1, kind=kind)
+    taps = formats.parse_filter_taps(str(tmp_path / "filter_taps.hpp"))
+    ref = formats.read_reference_bin(str(tmp_path / "reference.bin"))
+    assert ref.size == 1 << 12 and taps["n_sections"] == 4 and info["cross_check_rel"] <= 1e-4
+    design = formats.design_reference_filter(4, 0.1, kind)
+    np.testing.assert_array_equal(taps["sos"], design["sos"])
+    assert abs(taps["gain"] - design["gain"]) <= 1e-15 * abs(design["gain"])
+    x = formats.reference_input(ref.size, taps["gain"])
+    want = signal.sosfilt(taps["sos"].astype(np.float64), x.astype(np.float64)).astype(np.float32)
+    np.testing.assert_array_equal(ref, want)
+    assert ("Chebyshev" in open(tmp_path / "filter_taps.hpp").read()) == (kind == "cheby1")

@@ -246,3 +246,15 @@ def test_plr_repeated_launches(cuda_device):
         x = np.random.default_rng(i).uniform(-1, 1, n).astype(np.float32)
         e = oracle.errors(run_plan(plan, x), golden(sos, x))
         assert e["rel_max"] <= 1e-4, (i, n, e)
+
+
+@pytest.mark.parametrize("kind", ("butter", "cheby1"))
+@pytest.mark.parametrize("kernel", ("PH", "STCR_UNROLL", "DTCR_UNROLL", "TC", "PLR"))
+def test_check_reference_files(kind, kernel, tmp_path, cuda_device):
+    """The reference's generate-then-check flow on this library: reference.bin and
+    filter_taps.hpp written like tools/ref_generate.py, then the accuracy driver's gate
+    (src/test_accuracy.cu:178-188) through formats.check_reference_files."""
+    n_sections = 2 if kernel == "PLR" else 4  # the float32 direct form passes the gate to order 4
+    formats.generate_reference_files(str(tmp_path), n_sections, 16, cutoff=0.2, kind=kind)
+    res = formats.check_reference_files(str(tmp_path / "filter_taps.hpp"), str(tmp_path / "reference.bin"), kernel)
+    assert res["pass"], res
