@@ -285,8 +285,21 @@ struct CrBlock {
     // parity's samples).
     __device__ __forceinline__ static void write_row(float* buf, const float (&u)[NPAR][M], int r, int p0) {
         if (SPLIT) {
+            // The row's lane pair holds the even (p0 = 0) and odd (p0 = 1) samples. Float4 j is
+            // (e[2j], o[2j], e[2j+1], o[2j+1]); the even lane stores the even j, the odd lane the
+            // odd j. For each pair (j, j+1) each lane sends the two values its partner needs:
+            // the even lane e[2j+2], e[2j+3], the odd lane o[2j], o[2j+1].
 #pragma unroll(UNROLL ? 64 : 1)
-            for (int m = 0; m < M; ++m) buf[swz<N>(r, 2 * m + p0)] = u[0][m];
+            for (int j = 0; j < N / 4; j += 2) {
+                const float s0 = p0 ? u[0][2 * j] : u[0][2 * j + 2];
+                const float s1 = p0 ? u[0][2 * j + 1] : u[0][2 * j + 3];
+                const float r0 = __shfl_xor_sync(FULL_MASK, s0, 1);
+                const float r1 = __shfl_xor_sync(FULL_MASK, s1, 1);
+                const int jj = j + p0;  // the float4 this lane stores
+                const float4 v = p0 ? make_float4(r0, u[0][2 * j + 2], r1, u[0][2 * j + 3])
+                                    : make_float4(u[0][2 * j], r0, u[0][2 * j + 1], r1);
+                *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * jj)) = v;
+            }
         } else {
 #pragma unroll
             for (int j = 0; j < N / 4; ++j)
