@@ -1,9 +1,10 @@
-"""Autotuner for the plain realizations: picks realization and BLOCK_SIZE x N_BLOCKS geometry
+"""Autotuner for the realizations: picks realization and BLOCK_SIZE x N_BLOCKS geometry
 for a filter and signal length by timing the candidates on this GPU (CUDA events, device-
 resident data) and checking each against the FP64 reference filter on a prefix.
 
 The candidate order is a prior taken from measurements on GB300: at order 2 the two-pass
-single-section kernels, PH first; at higher orders PH with 64 samples per row. (The reference
+single-section kernels, PH first; for cascades the precision form (TC) first, then PH with 64
+samples per row. (The reference
 picks its launch shape from an occupancy model, gpu_specs.hpp:57-116; here the resident-block
 count comes from the CUDA occupancy query and the rest is measured.) Results are cached per
 (device, order, filter, signal-length bucket) in memory and, optionally, in a JSON file.
@@ -22,7 +23,7 @@ __all__ = ["tune", "tuned_plan"]
 
 _CANDIDATES_ORDER2 = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("STCR_UNROLL", 32, 32),
                       ("DTCR_UNROLL", 32, 64), ("PH", 32, 128), ("PLR", 0, 0)]
-_CANDIDATES_CASCADE = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("DTCR_UNROLL", 32, 64),
+_CANDIDATES_CASCADE = [("TC", 0, 0), ("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("DTCR_UNROLL", 32, 64),
                        ("PH", 32, 128), ("STCR_UNROLL", 32, 32)]
 _memo: dict = {}
 

@@ -335,10 +335,12 @@ int default_geometry(int kind, int n_sections, int& B, int& N) {
     return IIR_OK;
 }
 
+// Fastest realization by order, measured on GB300 at 2^28 samples: PH (two-pass) for orders 2
+// and 4 (697 / 369 GS/s); the precision form from order 8 (309 and 279 GS/s against PH's 247
+// and 152, with two to four times smaller error).
 int resolve_auto(int kernel, int n_sections) {
     if (kernel != IIR_KERNEL_AUTO) return kernel;
-    (void)n_sections;
-    return IIR_KERNEL_PH;
+    return n_sections >= 4 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
 }
 
 // samples per block (= per lookback unit)

@@ -45,7 +45,8 @@ extern "C" {
 #define IIR_ERR_TOO_LARGE        (-6)  /* n above the plan's capacity / 2^40 samples        */
 
 /* ---- realizations (reference: include/{ph,stcr,dtcr,plr}_kernels.cuh) ----------- */
-#define IIR_KERNEL_AUTO         0   /* fastest realization for the order (tuned on GB300) */
+#define IIR_KERNEL_AUTO         0   /* fastest realization for the order, measured on GB300:
+                                       PH to order 4, the precision form (TC) from order 8 */
 #define IIR_KERNEL_PH           1   /* PH_32 / PH_64                      ph_kernels.cuh:208,501   */
 #define IIR_KERNEL_STCR         2   /* STCR_*_LOOP (loop-form back-sub)   stcr_kernels.cuh:279,2586 */
 #define IIR_KERNEL_STCR_UNROLL  3   /* STCR_*_UNROLL_* (register form)    stcr_kernels.cuh:608-3605 */
