@@ -222,6 +222,19 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
     }
     for (int l = IIR_TAB_QG + 33; l < IIR_TAB_STRIDE; ++l) tab[l] = make_float4(0, 0, 0, 0);
     tab[IIR_TAB_HALF] = to_f4(mpow(A, static_cast<unsigned long long>(N / 2)));
+    // truncated lookback: the least m <= 4 with ||Q^m||_inf <= 1e-10 (a chunk's incoming state
+    // is then the sum of its m predecessors' aggregates to that bound), else 0
+    {
+        M2 Qm = Q;
+        int depth = 0;
+        for (int m = 1; m <= 4 && depth == 0; ++m) {
+            const double nrm = std::max(std::fabs(Qm.a) + std::fabs(Qm.b), std::fabs(Qm.c) + std::fabs(Qm.d));
+            if (std::isfinite(nrm) && nrm <= 1e-10) depth = m;
+            Qm = mmul(Qm, Q);
+        }
+        if (std::getenv("IIR_GB300_FULL_LOOKBACK")) depth = 0;
+        tab[IIR_TAB_LBD] = make_float4(static_cast<float>(depth), 0.f, 0.f, 0.f);
+    }
     return IIR_OK;
 }
 

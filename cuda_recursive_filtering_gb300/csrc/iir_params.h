@@ -21,12 +21,14 @@
 //   [TAB_QC + l]   = Q^l,      Q = A^(rows*N) (chunk transition), l <= 32
 //   [TAB_QG + l]   = Q^(32 l)  (group transition powers), l <= 32
 //   [TAB_HALF]     = A^(N/2)   (half-row transition)
+//   [TAB_LBD].x    = truncated lookback depth of the chunk transition (0: two-level lookback)
 #define IIR_GROUP 32
 #define IIR_TAB_CPOW 0
 #define IIR_TAB_GPOW 256
 #define IIR_TAB_QC 288
 #define IIR_TAB_QG 321
 #define IIR_TAB_HALF 354
+#define IIR_TAB_LBD 355  // .x: truncated lookback depth m (||Q^m|| <= 1e-10, m <= 4), 0 = full lookback
 #define IIR_TAB_STRIDE 356
 
 // Device-side per-plan launch state. `ticket` packs the launch epoch (the reference's

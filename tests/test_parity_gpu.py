@@ -258,3 +258,25 @@ def test_check_reference_files(kind, kernel, tmp_path, cuda_device):
     formats.generate_reference_files(str(tmp_path), n_sections, 16, cutoff=0.2, kind=kind)
     res = formats.check_reference_files(str(tmp_path / "filter_taps.hpp"), str(tmp_path / "reference.bin"), kernel)
     assert res["pass"], res
+
+
+@pytest.mark.parametrize("kernel", ("PH", "STCR_UNROLL", "DTCR_UNROLL"))
+@pytest.mark.parametrize("order", (4, 16))
+def test_cascade_truncated_and_two_level_lookback(kernel, order, monkeypatch, cuda_device):
+    """Cascades take the truncated lookback when a section's chunk transition has decayed
+    (||Q^m|| <= 1e-10, m <= 4) and the two-level decoupled lookback otherwise
+    (IIR_GB300_FULL_LOOKBACK forces it). Both meet the parity bar over many chunks."""
+    sos = butter(order, 0.05)
+    n = (1 << 22) + 333
+    x = np.random.default_rng(order).uniform(-1, 1, n).astype(np.float32)
+    ref = golden(sos, x)
+    outs = []
+    for full in (False, True):
+        if full:
+            monkeypatch.setenv("IIR_GB300_FULL_LOOKBACK", "1")
+        plan = Plan(sos, kernel, 32, 64, max_n=n)
+        y = run_plan(plan, x)
+        e = oracle.errors(y, ref)
+        assert e["rel_max"] <= 1e-4 and e["rel_rms"] <= RMS_TOL[order], (full, e)
+        outs.append(y)
+    assert np.max(np.abs(outs[0] - outs[1])) <= 1e-5 * np.max(np.abs(ref))
