@@ -348,12 +348,13 @@ int default_geometry(int kind, int n_sections, int& B, int& N) {
     return IIR_OK;
 }
 
-// Fastest realization by order, measured on GB300 at 2^28 samples: PH (two-pass) for orders 2
-// and 4 (697 / 369 GS/s); the precision form from order 8 (309 and 279 GS/s against PH's 247
-// and 152, with two to four times smaller error).
+// Fastest realization by order, measured on GB300 at 2^28 samples: PH up to order 8 (700 / 483 /
+// 321 GS/s at orders 2 / 4 / 8; the precision form gives 310 at order 8); the precision form from
+// order 10, its cost nearly flat in the order while PH's grows with the sections (order 16: 279
+// against 190 GS/s, with a quarter of the error).
 int resolve_auto(int kernel, int n_sections) {
     if (kernel != IIR_KERNEL_AUTO) return kernel;
-    return n_sections >= 4 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
+    return n_sections >= 5 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
 }
 
 // samples per block (= per lookback unit)
