@@ -60,9 +60,11 @@ struct BatchBlock {
         if (lane == 0 && !withhold) publish2(slots + static_cast<size_t>(lc) * 4, pf, t0, t1);
         float X0 = z0, X1 = z1;
         bool ok = true;
+        const int depth = static_cast<int>(tab[IIR_BT_LBD].x);  // truncated lookback depth (0: two-level)
         if (lc > 0)
-            ok = lookback_hier(p, slots, gslots, tab + IIR_BT_QC, tab + IIR_BT_QG, lc, epoch, t0, t1, withhold, X0, X1,
-                               z0, z1);
+            ok = depth > 0 ? lookback_trunc2(p, slots, tab + IIR_BT_QC, lc, epoch, depth, X0, X1, z0, z1)
+                           : lookback_hier(p, slots, gslots, tab + IIR_BT_QC, tab + IIR_BT_QG, lc, epoch, t0, t1,
+                                           withhold, X0, X1, z0, z1);
         if (lane == 0) {
             if (ok && !withhold) {
                 float f0, f1;
@@ -391,6 +393,7 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
                 tabs[base + IIR_BT_QC + l] = full[IIR_TAB_QC + l];
                 tabs[base + IIR_BT_QG + l] = full[IIR_TAB_QG + l];
             }
+            tabs[base + IIR_BT_LBD] = full[IIR_TAB_LBD];
         }
         max_sec = std::max(max_sec, ns);
         off += static_cast<size_t>(ns);

@@ -244,9 +244,11 @@ __device__ __forceinline__ bool lookback_give_up(const P& p, uint32_t epoch, uin
 // the signal contributing nothing. The host sets m only when ||Q^m||_inf <= 1e-10 (FP64), so the
 // neglected term Q^m X(c-m) is far below float32 resolution and a chunk waits for the aggregates
 // of its m predecessors only, never for a chain of inclusive carries. Lane i polls chunk c-1-i.
+// (z0, z1): the state before chunk 0 (a batched segment's initial state), whose term Q^c z is
+// kept while c < m.
 template <class P>
 __device__ bool lookback_trunc2(const P& p, const unsigned long long* slots, const float4* Qc, uint32_t c,
-                                uint32_t epoch, int m, float& X0, float& X1) {
+                                uint32_t epoch, int m, float& X0, float& X1, float z0 = 0.f, float z1 = 0.f) {
     const int lane = threadIdx.x & 31;
     const uint32_t pf = 2u * epoch + 1u;
     const bool mine = lane < m && static_cast<uint32_t>(lane) < c;
@@ -276,6 +278,12 @@ __device__ bool lookback_trunc2(const P& p, const unsigned long long* slots, con
             u0 = v0;
             u1 = v1;
         }
+    }
+    if (lane == 0 && c < static_cast<uint32_t>(m)) {
+        float w0, w1;
+        mv2(Qc[c], z0, z1, w0, w1);  // Q^c z
+        u0 += w0;
+        u1 += w1;
     }
     X0 = warp_sum(u0);
     X1 = warp_sum(u1);

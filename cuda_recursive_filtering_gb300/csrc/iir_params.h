@@ -115,6 +115,7 @@ struct IirPlrParams {
 #define IIR_BT_GPOW 128    // C^(t+1), t < 32
 #define IIR_BT_QC 160      // Q^l, l <= 32
 #define IIR_BT_QG 193      // Q^(32 l), l <= 32
+#define IIR_BT_LBD 226     // .x: truncated lookback depth (0: two-level lookback)
 #define IIR_BT_STRIDE 228
 
 struct IirBatchFilter {
