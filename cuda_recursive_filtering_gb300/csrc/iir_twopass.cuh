@@ -19,7 +19,7 @@
 //                     row tails; keeps the per-row zero-state incoming pairs for B (PH) and
 //                     publishes the chunk aggregate at once;
 //                  B: the realization's own solve of the chunk with its incoming state.
-// Every wait is bounded (iir_pipe.cuh: pipe_wait, lookback_hier).
+// Every wait is bounded (iir_pipe.cuh: pipe_wait, lookback_hier / lookback_trunc2).
 #pragma once
 #include "iir_pipe.cuh"
 
@@ -274,6 +274,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
         unsigned long long* slots = p.carry;
         unsigned long long* gslots = slots + static_cast<size_t>(p.carry_cap) * 4;
         const float4 Q = tc[G::TC_QC + 1];
+        const int lb_depth = static_cast<int>(p.tables[IIR_TAB_LBD].x);  // truncated lookback depth (0: two-level)
         const uint32_t ff = 2u * epoch + 2u;
         bool failed = false;
         for (uint32_t k = 0; k < nk; ++k) {
@@ -286,7 +287,9 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                 const float a0 = aux->partv[s][0], a1 = aux->partv[s][1];
                 const bool withhold = static_cast<long long>(c) == p.withhold_chunk;
                 if (c > 0)
-                    ok = lookback_hier(p, slots, gslots, tc + G::TC_QC, tc + G::TC_QG, c, epoch, a0, a1, withhold, X0, X1);
+                    ok = lb_depth > 0 ? lookback_trunc2(p, slots, tc + G::TC_QC, c, epoch, lb_depth, X0, X1)
+                                      : lookback_hier(p, slots, gslots, tc + G::TC_QC, tc + G::TC_QG, c, epoch, a0, a1,
+                                                      withhold, X0, X1);
                 if (lane == 0 && ok && !withhold) {
                     float q0, q1;
                     mv2(Q, X0, X1, q0, q1);
