@@ -280,7 +280,7 @@ def run_precision(dev, log2n: int) -> dict:
     return out
 
 
-def run_serving(dev, seconds: float = 2.0) -> dict:
+def run_serving(dev, seconds: float = 6.0) -> dict:
     """Continuous-batching stream server under Poisson arrivals (host chunks in, results back
     on the host): achieved GS/s and request latency percentiles."""
     from cuda_recursive_filtering_gb300 import workloads

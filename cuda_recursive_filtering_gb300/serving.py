@@ -238,8 +238,10 @@ class StreamServer:
     def latency_percentiles(self, qs=(50, 99)) -> dict:
         lat = np.array([r.latency for r in self.completed if r.latency is not None])
         if lat.size == 0:
-            return {f"p{q}_us": None for q in qs}
-        return {f"p{q}_us": float(np.percentile(lat, q) * 1e6) for q in qs}
+            return {**{f"p{q}_us": None for q in qs}, "max_us": None}
+        out = {f"p{q}_us": float(np.percentile(lat, q) * 1e6) for q in qs}
+        out["max_us"] = float(lat.max() * 1e6)
+        return out
 
 
 def run_poisson_load(server: StreamServer, streams: list[int], rate_sps: float, duration_s: float,
