@@ -19,9 +19,10 @@ def butter(order, cutoff=0.1):
 
 
 @pytest.mark.parametrize("kernel,order", [("PH", 4), ("PH", 2), ("DTCR_UNROLL", 4), ("DTCR_UNROLL", 2), ("STCR", 4), ("STCR", 2),
-                                          ("PLR", 4)])
+                                          ("PLR", 4), ("TC", 8), ("TC", 16)])
 def test_withheld_carry_times_out_and_plan_recovers(kernel, order, cuda_device):
-    """Order 2 runs the single-section persistent pipeline, order 4 the per-chunk blocks."""
+    """Order 2 runs the single-section persistent pipeline, order 4 the per-chunk blocks, TC the
+    precision form's tile pipeline (chunk 7 = tile 7)."""
     sos = butter(order)
     n = 1 << 20
     x = np.random.default_rng(0).uniform(-1, 1, n).astype(np.float32)

@@ -96,3 +96,17 @@ def test_tc_long_signal(order, cuda_device):
         y = plan(xt)
     plan.check()
     _check(y.cpu().numpy(), xt.cpu().numpy(), sos)
+
+
+@pytest.mark.parametrize("order,cutoff", [(8, 0.02), (16, 0.05), (16, 0.3)])
+def test_tc_cheby1(order, cutoff, cuda_device):
+    """Chebyshev type I (1 dB ripple): poles closer to the unit circle than Butterworth's of the
+    same order, the harder case for the state basis."""
+    from scipy import signal
+    sos = signal.cheby1(order, 1.0, cutoff, output="sos")
+    n = (1 << 21) + 5
+    x = np.random.default_rng(order).uniform(-1, 1, n).astype(np.float32)
+    plan = Plan(sos, "TC", max_n=n)
+    y = plan(torch.from_numpy(x).cuda())
+    plan.check()
+    _check(y.cpu().numpy(), x, sos, rms_tol=2e-5)
