@@ -806,14 +806,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 }
                 S = step(S, j, xhp + j * 2, vx);
             }
-            if (D + 2 > 16 && d < 2) {  // D = 16: history columns 16, 17 by lanes 0, 1
-                for (int i = 0; i < TC_SUB; ++i) {
-                    const int j = grp * TC_SUB + i;
-                    const float v = xhp[j * 2 + d];
-                    const float h = tf32_hi(v);
-                    a2s[swz32(j, D + d)] = h;
-                    a2s[TC_KB + swz32(j, D + d)] = tf32_hi(v - h);
-                }
+            if (D + 2 > 16) {  // D = 16: history columns 16, 17 of the 8 chunks, one per lane
+                const int j = grp * TC_SUB + (d >> 1), e = d & 1;
+                const float v = xhp[j * 2 + e];
+                const float h = tf32_hi(v);
+                a2s[swz32(j, D + e)] = h;
+                a2s[TC_KB + swz32(j, D + e)] = tf32_hi(v - h);
             }
             fence_proxy_async_smem();
             tc_fence_before();
