@@ -687,14 +687,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             aux->Ig0[k % TC_NACC][grp][d] = grp > 0 ? Vc[(grp - 1) * TC_DMAX + d] : 0.f;
             if (grp == TC_GROUPS - 1) aux->agg[k % TC_NS][d] = Vc[grp * TC_DMAX + d];
             bar_group(1);
-            if (ct == 0) {
+            if (ct < KD / 2) {  // the aggregate's part words, one pair per lane
                 const uint32_t t = tile_of(k);
                 if (static_cast<long long>(t) != p.withhold_chunk) {
-                    float a[KD];
-#pragma unroll
-                    for (int e = 0; e < KD; ++e) a[e] = aux->agg[k % TC_NS][e];
-                    publishk<KD>(slots + static_cast<size_t>(t) * 2 * KD, 2u * epoch + 1u, a);
+                    const uint32_t pf = 2u * epoch + 1u;
+                    st_relaxed_v2(slots + static_cast<size_t>(t) * 2 * KD + 2 * ct,
+                                  pack_word(pf, aux->agg[k % TC_NS][2 * ct]), pack_word(pf, aux->agg[k % TC_NS][2 * ct + 1]));
                 }
+            }
+            if (ct == 0) {
                 mbar_arrive(&aux->mb_agg[k % TC_NS]);
                 TC_STAMP(k, 5);
             }
