@@ -131,10 +131,10 @@ struct BatchBlock {
 #pragma unroll
             for (int k = 0; k < PER; ++k) {
                 const int i = tid + k * THREADS;
-                if (i < V) *reinterpret_cast<float4*>(buf + swz<N>((4 * i) / N, (4 * i) % N)) = v[k];
+                if (i < V) *reinterpret_cast<float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N)) = v[k];
             }
         } else {
-            for (int i = tid; i < CHUNK; i += THREADS) buf[swz<N>(i / N, i % N)] = (i < nrem) ? sg.x[cs + i] : 0.f;
+            for (int i = tid; i < CHUNK; i += THREADS) buf[swz<N, ROWS, true>(i / N, i % N)] = (i < nrem) ? sg.x[cs + i] : 0.f;
         }
         __syncthreads();
 
@@ -145,8 +145,8 @@ struct BatchBlock {
         float xh2 = 0.f, xh1 = 0.f;
         if (row_warp) {
             if (r > 0) {
-                xh2 = buf[swz<N>(r - 1, N - 2)];
-                xh1 = buf[swz<N>(r - 1, N - 1)];
+                xh2 = buf[swz<N, ROWS, true>(r - 1, N - 2)];
+                xh1 = buf[swz<N, ROWS, true>(r - 1, N - 1)];
             } else if (lc > 0) {
                 xh2 = sg.x[cs - 2];
                 xh1 = sg.x[cs - 1];
@@ -160,7 +160,7 @@ struct BatchBlock {
             if (gain != 1.f) {
 #pragma unroll 4
                 for (int j = 0; j < N / 4; ++j) {
-                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
                     const float4 v = *ptr;
                     *ptr = make_float4(v.x * gain, v.y * gain, v.z * gain, v.w * gain);
                 }
@@ -231,7 +231,7 @@ struct BatchBlock {
                                 e2 = e1;
                                 e1 = dn;
                             }
-                            sg.zf[2 + 2 * sec + t] = buf[swz<N>(r, static_cast<int>(m - rs))] + dn;
+                            sg.zf[2 + 2 * sec + t] = buf[swz<N, ROWS, true>(r, static_cast<int>(m - rs))] + dn;
                         }
                     }
                     // the second-to-last sample in the previous chunk: the chunk's incoming y[-1]
@@ -251,9 +251,9 @@ struct BatchBlock {
         if (cnt == CHUNK && (reinterpret_cast<uintptr_t>(sg.y) & 15u) == 0) {
             float4* dst = reinterpret_cast<float4*>(sg.y + cs);
             for (int i = tid; i < CHUNK / 4; i += THREADS)
-                dst[i] = *reinterpret_cast<const float4*>(buf + swz<N>((4 * i) / N, (4 * i) % N));
+                dst[i] = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N));
         } else {
-            for (int i = tid; i < cnt; i += THREADS) sg.y[cs + i] = buf[swz<N>(i / N, i % N)];
+            for (int i = tid; i < cnt; i += THREADS) sg.y[cs + i] = buf[swz<N, ROWS, true>(i / N, i % N)];
         }
         if (sg.zf && tid == 0 && nrem <= CHUNK) {
             // input history after the segment (raw)

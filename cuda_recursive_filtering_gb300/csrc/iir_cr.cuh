@@ -18,10 +18,12 @@
 // (the reference's "block filtering", here a Kogge-Stone scan per parity). Back-substitution
 // then recovers the dropped positions level by level:
 //     y[d] = u[d] - c_k y[d - h] - d_k y[d - 3h],   c_k = e_k - f_k/e_k,  d_k = -f_k^2/e_k.
-// All of this runs in the zero-padded chunk (zero state before the chunk); the response to
-// the chunk's incoming state is added afterwards (PH-style correction), which keeps the
-// chunk-boundary algebra simple (the reference folds it into the back-substitution with
-// the h/g/p/q factors, stcr_kernels.cuh:479-585).
+// In the cascade kernels this runs in the zero-padded tile (zero state before the tile) and
+// the response to the tile's incoming state is added afterwards (PH-style correction), since
+// that state is only known after the lookback. The two-pass kernels know it before the solve
+// and put it into the first row's right-hand sides instead (solve_tile, Y2 / Y1). The
+// reference folds the state into the back-substitution with its h/g/p/q factors
+// (stcr_kernels.cuh:479-585).
 //
 // UNROLL selects the register form (literal indices; the reference's hand-unrolled kernels)
 // or the loop form (run-time loops over a thread-local array; the reference's *_LOOP
@@ -82,7 +84,7 @@ constexpr int ilog2_c(int v) { return v <= 1 ? 0 : 1 + ilog2_c(v / 2); }
 // S_w = C^(RW w) X + sum_{v<w} C^(RW (w-1-v)) P_v (P_v = tile v's zero-state end pair,
 // X = the chunk's incoming state from the lookback), and every row adds the response of the
 // section recurrence to its own incoming pair C^(row) S_w.
-template <bool SPLIT, int B_, int N_, int ROWS_, bool UNROLL>
+template <bool SPLIT, int B_, int N_, int ROWS_, bool UNROLL, bool PLANES = true>
 struct CrBlock {
     static constexpr int B = B_, N = N_, ROWS = ROWS_, M = N_ / 2, L = ilog2_c(N_);
     static constexpr int TPR = SPLIT ? 2 : 1;   // threads per row
@@ -124,9 +126,15 @@ struct CrBlock {
     // back-substitution. (P0, P1) = the tile's zero-state end pair (valid in its last row).
     // Xp0/Xp1: the previous section's incoming state (row-0 input history for sec > 0).
     // h2, h1: the two input samples before the chunk (row 0's history in section 0).
+    // (Y2, Y1) = (y[-2], y[-1]) before the tile's first row: zero for the zero-padded tile; a
+    // known incoming pair enters the stride-2 system through its first four right-hand sides
+    //     v[0] = y[0],  v[1] = y[1],  v[2] -= f_1 y[-2],  v[3] -= f_1 y[-1]
+    // (y[0], y[1] from the section recurrence), after which the zero-padded solve returns the
+    // true output of the tile.
     __device__ __forceinline__ static void solve_tile(const IirParams& p, const float* buf, const IirSection& q, int sec,
                                                       float h2, float h1, int r, int rl, int p0, float Xp0,
-                                                      float Xp1, float (&u)[NPAR][M], float& P0, float& P1) {
+                                                      float Xp1, float Y2, float Y1, float (&u)[NPAR][M], float& P0,
+                                                      float& P1) {
         float s0[NPAR], s1[NPAR];
         // ---- FIR + first double-sided round -> u (own parity halves) ----
         const float g = (sec == 0) ? p.gain : 1.f;
@@ -136,10 +144,10 @@ struct CrBlock {
             // the lane only (no per-sample selects).
             float m4, m3, m2, m1;  // raw x[-4], x[-3], x[-2], x[-1] of this row
             if (r > 0) {
-                m4 = buf[swz<N>(r - 1, N - 4)];
-                m3 = buf[swz<N>(r - 1, N - 3)];
-                m2 = buf[swz<N>(r - 1, N - 2)];
-                m1 = buf[swz<N>(r - 1, N - 1)];
+                m4 = buf[swz<N, ROWS, PLANES>(r - 1, N - 4)];
+                m3 = buf[swz<N, ROWS, PLANES>(r - 1, N - 3)];
+                m2 = buf[swz<N, ROWS, PLANES>(r - 1, N - 2)];
+                m1 = buf[swz<N, ROWS, PLANES>(r - 1, N - 1)];
             } else {
                 m4 = m3 = 0.f;
                 m2 = (sec == 0) ? h2 : Xp0;
@@ -152,7 +160,7 @@ struct CrBlock {
             float xr0 = 0.f, xr1 = 0.f;  // raw x[0], x[1] of the row
 #pragma unroll
             for (int j = 0; j < N / 4; ++j) {
-                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
                 if (j == 0) {
                     xr0 = v4.x;
                     xr1 = v4.y;
@@ -165,19 +173,23 @@ struct CrBlock {
                 m1 = v4.w;
             }
             if (rl == 0) {
-                // zero-padded tile: the FIR output before the tile counts as zero, so
-                // v1[0] = w[0] and v1[1] = w[1] - e w[0]
+                // first row of the tile: y[0] = w[0] + a1 y[-1] + a2 y[-2], y[1] = w[1] + a1 y[0] + a2 y[-1]
+                // (v[0], v[1] of the system that is zero before the tile), and f_1 y[n-4] moved out of
+                // v[2], v[3]
                 const float w0 = g * fmaf(q.b2, xm2, fmaf(q.b1, xm1, xr0));
                 const float w1 = g * fmaf(q.b2, xm1, fmaf(q.b1, xr0, xr1));
-                u[0][0] = p0 ? fmaf(-q.e0, w0, w1) : w0;
+                const float y0 = fmaf(q.a1, Y1, fmaf(q.a2, Y2, w0));
+                const float y1 = fmaf(q.a1, y0, fmaf(q.a2, Y1, w1));
+                u[0][0] = p0 ? y1 : y0;
+                u[0][1] = fmaf(q.ha2, p0 ? Y1 : Y2, u[0][1]);
             }
         } else {
             float x1, x2, x3, x4;  // x[-1], x[-2], x[-3], x[-4] of this row
             if (r > 0) {
-                x4 = buf[swz<N>(r - 1, N - 4)] * g;
-                x3 = buf[swz<N>(r - 1, N - 3)] * g;
-                x2 = buf[swz<N>(r - 1, N - 2)] * g;
-                x1 = buf[swz<N>(r - 1, N - 1)] * g;
+                x4 = buf[swz<N, ROWS, PLANES>(r - 1, N - 4)] * g;
+                x3 = buf[swz<N, ROWS, PLANES>(r - 1, N - 3)] * g;
+                x2 = buf[swz<N, ROWS, PLANES>(r - 1, N - 2)] * g;
+                x1 = buf[swz<N, ROWS, PLANES>(r - 1, N - 1)] * g;
             } else if (sec == 0) {
                 x4 = x3 = 0.f;
                 x2 = h2 * g;
@@ -193,7 +205,7 @@ struct CrBlock {
             float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
 #pragma unroll
             for (int j = 0; j < N / 4; ++j) {
-                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N>(r, 4 * j));
+                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
                 const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -205,6 +217,15 @@ struct CrBlock {
                     w2 = w1;
                     w1 = wn;
                 }
+            }
+            if (rl == 0) {
+                // first row of the tile: v[0] = y[0], v[1] = y[1] and f_1 y[n-4] moved out of v[2], v[3]
+                // (the loop above left v[0] = w[0], v[1] = w[1] + a1 w[0])
+                const float dy0 = fmaf(q.a1, Y1, q.a2 * Y2);
+                u[0][0] += dy0;
+                u[1][0] = fmaf(q.a1, dy0, fmaf(q.a2, Y1, u[1][0]));
+                u[0][1] = fmaf(q.ha2, Y2, u[0][1]);
+                u[1][1] = fmaf(q.ha2, Y1, u[1][1]);
             }
         }
         // ---- elimination levels 1 .. L-1 (previous row's kept tail by shuffle) ----
@@ -298,12 +319,12 @@ struct CrBlock {
                 const int jj = j + p0;  // the float4 this lane stores
                 const float4 v = p0 ? make_float4(r0, u[0][2 * j + 2], r1, u[0][2 * j + 3])
                                     : make_float4(u[0][2 * j], r0, u[0][2 * j + 1], r1);
-                *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * jj)) = v;
+                *reinterpret_cast<float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * jj)) = v;
             }
         } else {
 #pragma unroll
             for (int j = 0; j < N / 4; ++j)
-                *reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j)) =
+                *reinterpret_cast<float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j)) =
                     make_float4(u[0][2 * j], u[1][2 * j], u[0][2 * j + 1], u[1][2 * j + 1]);
         }
     }
@@ -329,7 +350,7 @@ struct CrBlock {
             const float4 Ct = tab[IIR_TAB_CPOW + RW - 1];  // tile transition C^RW
             float P0 = 0.f, P1 = 0.f;  // tile zero-state end pair (valid in the tile's last row)
             if (row_warp) {
-                solve_tile(p, buf, q, sec, h2, h1, r, rl, p0, Xp0, Xp1, u, P0, P1);
+                solve_tile(p, buf, q, sec, h2, h1, r, rl, p0, Xp0, Xp1, 0.f, 0.f, u, P0, P1);
                 if (lane == 31) {
                     aux->wtot[w][0][0] = P0;
                     aux->wtot[w][0][1] = P1;
@@ -370,40 +391,33 @@ struct CrBlock {
 
 
 // Single-section STCR / DTCR on the two-pass pipeline (iir_twopass.cuh): pass B is CrBlock's
-// section solve with the chunk's incoming state known from the start (tile solve, tile join,
-// response to the incoming state added in registers, one write of each row).
+// tile solve with the tile's true incoming pair known from the start. Pass A left every row's
+// zero-state incoming pair (zin), so tile w starts from S_w = zin[RW w] + C^(RW w) X; the solve
+// takes S_w in its first row's right-hand sides and returns the true output, which each row
+// writes once (no tile join, no response added afterwards).
 template <bool SPLIT, int N_, int ROWS_, bool UNROLL>
 struct CrTwo {
-    using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL>;
+    using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL, IIR_TWO_PLANES>;
     static constexpr int N = N_, ROWS = ROWS_, M = Blk::M, NPAR = Blk::NPAR, RW = Blk::RW, NW = Blk::NW;
     static constexpr int TPR = Blk::TPR;
 
     __device__ static void b_pass(const IirParams& p, float* buf, const float* hist, const float4* tc,
-                                  const float (*)[2], PipeAux* aux, float X0, float X1, int w, int lane) {
+                                  const float (*zin)[2], PipeAux*, float X0, float X1, int w, int lane) {
         const int rl = SPLIT ? (lane >> 1) : lane;
         const int r = w * RW + rl;
         const int p0 = SPLIT ? (lane & 1) : 0;
         const IirSection& q = p.sec[0];
-        float u[NPAR][M];
-        float P0, P1;
-        Blk::solve_tile(p, buf, q, 0, hist[30], hist[31], r, rl, p0, 0.f, 0.f, u, P0, P1);
-        if (lane == 31) {
-            aux->wtot[w][0][0] = P0;
-            aux->wtot[w][0][1] = P1;
-        }
-        named_barrier_rows(NW);  // every row read its input history; tile end pairs visible
-        float in0, in1;
-        warp_incoming(aux, w, 0, tc[RW - 1], in0, in1);  // C^RW across a tile
-        float S0 = X0, S1 = X1;
+        float S0 = X0, S1 = X1;  // (y[-2], y[-1]) before the tile's first row
         if (w > 0) {
             float t0, t1;
             mv2(tc[RW * w - 1], X0, X1, t0, t1);  // C^(RW w)
-            S0 = t0 + in0;
-            S1 = t1 + in1;
+            S0 = t0 + zin[RW * w][0];
+            S1 = t1 + zin[RW * w][1];
         }
-        float d2 = S0, d1 = S1;
-        if (rl > 0) mv2(tc[rl - 1], S0, S1, d2, d1);  // C^rl
-        Blk::add_response(u, q, p0, d2, d1);
+        float u[NPAR][M];
+        float P0, P1;
+        Blk::solve_tile(p, buf, q, 0, hist[30], hist[31], r, rl, p0, 0.f, 0.f, S0, S1, u, P0, P1);
+        named_barrier_rows(NW);  // every row has read its input history
         Blk::write_row(buf, u, r, p0);
     }
 };

@@ -488,12 +488,21 @@ constexpr int min_blocks_for(size_t smem_bytes, int threads) {
 }
 
 // Float index of sample n of row r in the swizzled chunk buffer (128B swizzle: the 16-byte
-// unit u of line L lives at unit u ^ (L & 7)).
-template <int N>
+// unit u of line L lives at unit u ^ (L & 7)). Two layouts:
+//   PLANES  rows of 32 or more samples stored as N / 32 planes of 32-sample columns,
+//           plane-major ([N/32][ROWS][32]): line L = plane * ROWS + r, so L & 7 = r & 7 and the
+//           32 rows a warp reads at one column fall on 8 distinct units (four wavefronts per
+//           128-bit access, no bank conflict). Each plane is one tensor copy.
+//   lines   the chunk as it lies in memory, CHUNK / 32 lines of 32 samples: L = r * N / 32 +
+//           n / 32, one tensor copy per chunk. For N = 64 (128) only 4 (2) of the 8 units are
+//           used at a column: 2-way (4-way) conflicts for a warp of rows.
+// Rows of 16 samples share a line (two rows per line) in both.
+template <int N, int ROWS, bool PLANES>
 __device__ __forceinline__ int swz(int r, int n) {
+    static_assert(ROWS % 8 == 0, "whole swizzle atoms per plane");
     int L, u;
     if constexpr (N >= 32) {
-        L = r * (N / 32) + (n >> 5);
+        L = PLANES ? (n >> 5) * ROWS + r : r * (N / 32) + (n >> 5);
         u = (n & 31) >> 2;
     } else {
         L = r >> 1;
@@ -532,6 +541,29 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
                  : "memory");
 }
 
+// Chunk c between global memory and its swizzled buffer. PLANES: one tensor copy per plane
+// (the map views the signal as rows of N samples, box 32 x ROWS); lines: one copy of CHUNK / 32
+// lines (the map views the signal as 32-sample lines). 128B swizzle in both.
+template <int ROWS, int N, bool PLANES>
+__device__ __forceinline__ void tma_load_chunk(float* buf, const CUtensorMap* map, uint32_t c,
+                                               unsigned long long* bar) {
+    if constexpr (PLANES && N >= 32) {
+#pragma unroll
+        for (int h = 0; h < N / 32; ++h) tma_load_2d(buf + h * ROWS * 32, map, 32 * h, static_cast<int>(c) * ROWS, bar);
+    } else {
+        tma_load_2d(buf, map, 0, static_cast<int>(c) * (ROWS * N / 32), bar);
+    }
+}
+template <int ROWS, int N, bool PLANES>
+__device__ __forceinline__ void tma_store_chunk(const CUtensorMap* map, uint32_t c, const float* buf) {
+    if constexpr (PLANES && N >= 32) {
+#pragma unroll
+        for (int h = 0; h < N / 32; ++h) tma_store_2d(map, 32 * h, static_cast<int>(c) * ROWS, buf + h * ROWS * 32);
+    } else {
+        tma_store_2d(map, 0, static_cast<int>(c) * (ROWS * N / 32), buf);
+    }
+}
+
 // Control warp: takes the ticket and starts the chunk's TMA load.
 template <int ROWS, int N>
 __device__ __forceinline__ void block_begin(const IirParams& p, float* buf, BlockAux* aux) {
@@ -545,7 +577,7 @@ __device__ __forceinline__ void block_begin(const IirParams& p, float* buf, Bloc
         aux->bail = 0;
         if (chunk_is_bulk<ROWS, N>(p, c)) {
             mbar_arrive_expect_tx(&aux->mbar, static_cast<uint32_t>(BlockGeom<ROWS, N>::DATA_BYTES));
-            tma_load_2d(buf, &p.tmap_x, 0, static_cast<int>(c) * BlockGeom<ROWS, N>::LINES, &aux->mbar);
+            tma_load_chunk<ROWS, N, true>(buf, &p.tmap_x, c, &aux->mbar);
         }
     }
 }
@@ -565,7 +597,7 @@ __device__ __forceinline__ bool block_acquire(const IirParams& p, float* buf, Bl
         const long long cs = static_cast<long long>(c) * (ROWS * N);
         for (int i = threadIdx.x; i < ROWS * N; i += THREADS) {
             const long long g = cs + i;
-            buf[swz<N>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
+            buf[swz<N, ROWS, true>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
         }
         __syncthreads();
     }
@@ -578,7 +610,7 @@ template <int ROWS, int N, int THREADS>
 __device__ __forceinline__ void block_store(const IirParams& p, float* buf, uint32_t c) {
     if (chunk_is_bulk<ROWS, N>(p, c)) {
         if (threadIdx.x == 0) {
-            tma_store_2d(&p.tmap_y, 0, static_cast<int>(c) * BlockGeom<ROWS, N>::LINES, buf);
+            tma_store_chunk<ROWS, N, true>(&p.tmap_y, c, buf);
             bulk_commit();
             bulk_wait_read_all();  // shared memory must outlive the copy's reads
         }
@@ -586,7 +618,7 @@ __device__ __forceinline__ void block_store(const IirParams& p, float* buf, uint
         const long long cs = static_cast<long long>(c) * (ROWS * N);
         for (int i = threadIdx.x; i < ROWS * N; i += THREADS) {
             const long long g = cs + i;
-            if (g < p.n) p.y[g] = buf[swz<N>(i / N, i % N)];
+            if (g < p.n) p.y[g] = buf[swz<N, ROWS, true>(i / N, i % N)];
         }
     }
 }

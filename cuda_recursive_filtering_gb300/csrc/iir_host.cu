@@ -284,6 +284,18 @@ bool encode_rows_map(CUtensorMap* map, const float* base, long long rows, int ro
     return r == CUDA_SUCCESS;
 }
 
+// The view a chunk kernel's tensor copies use (tma_load_chunk / tma_store_chunk): with planes,
+// rows of n_per_row >= 32 samples, box 32 x rows_per_chunk (one copy per 32-sample plane);
+// otherwise (and for 16-sample rows) 32-sample lines, box = the chunk's lines.
+bool encode_chunk_map(CUtensorMap* map, const float* base, long long n, int n_per_row, int rows_per_chunk,
+                      bool planes) {
+    if (planes && n_per_row >= 32) {
+        if (n < n_per_row) return false;
+        return encode_rows_map(map, base, n / n_per_row, n_per_row, 32, rows_per_chunk);
+    }
+    return encode_lines_map(map, base, n, rows_per_chunk * n_per_row / 32);
+}
+
 // Same view with a one-line box and no swizzle: the 32 samples before a chunk.
 bool encode_hist_map(CUtensorMap* map, const float* base, long long n) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
@@ -682,9 +694,10 @@ int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stre
         q.nchunks = static_cast<unsigned int>(nchunks);
         q.carry_cap = static_cast<unsigned int>(p->carry_cap);
         q.carry_stride = carry_words_per_section(p, p->carry_cap);
-        const int lines = static_cast<int>(chunk / 32);
-        q.use_tma = (aligned && encode_lines_map(&q.tmap_x, x, static_cast<long long>(n), lines) &&
-                     encode_lines_map(&q.tmap_y, y, static_cast<long long>(n), lines) &&
+        const int npr = p->entry->N, rows = p->entry->rows;
+        const bool planes = p->entry->planes != 0;
+        q.use_tma = (aligned && encode_chunk_map(&q.tmap_x, x, static_cast<long long>(n), npr, rows, planes) &&
+                     encode_chunk_map(&q.tmap_y, y, static_cast<long long>(n), npr, rows, planes) &&
                      (!p->entry->pipeline || encode_hist_map(&q.tmap_h, x, static_cast<long long>(n))))
                         ? 1
                         : 0;

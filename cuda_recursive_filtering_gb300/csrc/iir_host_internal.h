@@ -28,6 +28,9 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
 bool encode_lines_map(CUtensorMap* map, const float* base, long long n, int lines_per_block);
 // 2D tensor map over rows of row_len floats, box {box_inner, box_rows}, 128-byte swizzle.
 bool encode_rows_map(CUtensorMap* map, const float* base, long long rows, int row_len, int box_inner, int box_rows);
+// The chunk kernels' view: rows of n_per_row samples (one box per 32-sample plane), or lines.
+bool encode_chunk_map(CUtensorMap* map, const float* base, long long n, int n_per_row, int rows_per_chunk,
+                      bool planes);
 // cudaError_t -> IIR_* status (clears the runtime's sticky last error).
 int cuda_status(cudaError_t e);
 

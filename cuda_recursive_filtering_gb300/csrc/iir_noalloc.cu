@@ -138,10 +138,9 @@ extern "C" int iir_sos_filter_noalloc(const float* x, float* y, size_t n, const 
     q.gain = static_cast<float>(gain);
     q.timeout_ns = 1000000000ll;
     q.withhold_chunk = -1;
-    const int lines = static_cast<int>(NA_CHUNK / 32);
     const bool aligned = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15u) == 0;
-    q.use_tma = (aligned && encode_lines_map(&q.tmap_x, x, static_cast<long long>(n), lines) &&
-                 encode_lines_map(&q.tmap_y, y, static_cast<long long>(n), lines))
+    q.use_tma = (aligned && encode_chunk_map(&q.tmap_x, x, static_cast<long long>(n), NA_N, e->rows, e->planes != 0) &&
+                 encode_chunk_map(&q.tmap_y, y, static_cast<long long>(n), NA_N, e->rows, e->planes != 0))
                     ? 1
                     : 0;
     void* args[] = {&q};

@@ -60,7 +60,7 @@ struct IirSection {
 };
 
 struct IirParams {
-    CUtensorMap tmap_x;               // 2D view of x as 32-float lines, 128B swizzle (bulk path)
+    CUtensorMap tmap_x;               // 2D view of x as rows of N samples, box 32 x rows, 128B swizzle (bulk path)
     CUtensorMap tmap_y;
     CUtensorMap tmap_h;               // persistent pipeline: one 32-float line, no swizzle (input history)
     const float* x;

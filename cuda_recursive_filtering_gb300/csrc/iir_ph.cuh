@@ -56,7 +56,7 @@ struct PhBlock {
         float y1 = 0.f, y2 = 0.f;
 #pragma unroll 4
         for (int j = 0; j < N / 4; ++j) {
-            float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+            float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
             const float4 q = *ptr;
             const float xs[4] = {q.x, q.y, q.z, q.w};
             float ys[4];
@@ -87,7 +87,7 @@ struct PhBlock {
     __device__ static void correct_pass(float* buf, int r, float a1, float a2, float d2, float d1) {
 #pragma unroll 4
         for (int j = 0; j < N / 4; ++j) {
-            float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+            float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
             const float4 q = *ptr;
             float v[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
@@ -111,8 +111,8 @@ struct PhBlock {
         const float gain = p.gain;
         if (row_warp) {
             if (r > 0) {
-                xh2 = buf[swz<N>(r - 1, N - 2)];
-                xh1 = buf[swz<N>(r - 1, N - 1)];
+                xh2 = buf[swz<N, ROWS, true>(r - 1, N - 2)];
+                xh1 = buf[swz<N, ROWS, true>(r - 1, N - 1)];
             } else if (c > 0) {
                 const long long cs = static_cast<long long>(c) * (ROWS * N);
                 xh2 = __ldg(p.x + cs - 2);
@@ -125,7 +125,7 @@ struct PhBlock {
             if (gain != 1.f) {
 #pragma unroll 4
                 for (int j = 0; j < N / 4; ++j) {
-                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
                     const float4 q = *ptr;
                     *ptr = make_float4(q.x * gain, q.y * gain, q.z * gain, q.w * gain);
                 }
@@ -213,8 +213,8 @@ struct PhTwo {
         const float gain = p.gain;
         float xh2, xh1;
         if (r > 0) {
-            xh2 = buf[swz<N>(r - 1, N - 2)];
-            xh1 = buf[swz<N>(r - 1, N - 1)];
+            xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 2)];
+            xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 1)];
         } else {
             xh2 = hist[30];
             xh1 = hist[31];
@@ -231,7 +231,7 @@ struct PhTwo {
         named_barrier_rows(NW);  // every row has its input history before rows are overwritten
 #pragma unroll 4
         for (int j = 0; j < N / 4; ++j) {
-            float4* ptr = reinterpret_cast<float4*>(buf + swz<N>(r, 4 * j));
+            float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, IIR_TWO_PLANES>(r, 4 * j));
             const float4 v = *ptr;
             const float xs[4] = {v.x * gain, v.y * gain, v.z * gain, v.w * gain};
             float ys[4];

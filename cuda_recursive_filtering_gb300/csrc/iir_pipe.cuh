@@ -17,6 +17,12 @@ namespace iirgb {
 #define IIR_PIPE_ROWS_N128 64
 #endif
 
+// Shared-memory layout of the single-section pipelines' chunk buffers (swz in iir_device.cuh):
+// 0 = lines (one tensor copy per chunk, contiguous in memory), 1 = planes of 32-sample columns.
+#ifndef IIR_TWO_PLANES
+#define IIR_TWO_PLANES 0
+#endif
+
 struct PipeAux {
     unsigned long long full[8];
     unsigned long long part[8];

@@ -28,6 +28,7 @@ struct KernelEntry {
     int order;      // PLR direct-form order (0 for the cascaded realizations)
     int rows;       // rows per block (tiles x B) for the row-major realizations
     int pipeline = 0;  // 1: single-section persistent pipeline, launched cooperatively
+    int planes = 1;    // chunk buffer layout: 1 = planes of 32-sample columns, 0 = lines (swz)
 };
 
 void register_ph(std::vector<KernelEntry>& reg);

@@ -82,25 +82,24 @@ __device__ __forceinline__ void pass_aggregate(const IirParams& p, const float* 
     static_assert(NW * RW == ROWS, "rows per block");
     const int rl = lane / TPR, p0 = lane % TPR, r = w * RW + rl, n0 = p0 * SPAN;
     const IirSection& q = p.sec[0];
-    const float gain = p.gain;
     float xh2, xh1;
     if (n0 > 0) {
-        xh2 = buf[swz<N>(r, n0 - 2)];
-        xh1 = buf[swz<N>(r, n0 - 1)];
+        xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r, n0 - 2)];
+        xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r, n0 - 1)];
     } else if (r > 0) {
-        xh2 = buf[swz<N>(r - 1, N - 2)];
-        xh1 = buf[swz<N>(r - 1, N - 1)];
+        xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 2)];
+        xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 1)];
     } else {
         xh2 = hist[30];
         xh1 = hist[31];
     }
-    xh2 *= gain;
-    xh1 *= gain;
+    // The aggregate is linear in the input: the recurrence runs on the raw samples and the
+    // gain scales its end pair once.
     float y1 = 0.f, y2 = 0.f;
 #pragma unroll 4
     for (int j = 0; j < SPAN / 4; ++j) {
-        const float4 v = *reinterpret_cast<const float4*>(buf + swz<N>(r, n0 + 4 * j));
-        const float xs[4] = {v.x * gain, v.y * gain, v.z * gain, v.w * gain};
+        const float4 v = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, IIR_TWO_PLANES>(r, n0 + 4 * j));
+        const float xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const float wv = fmaf(q.b2, xh2, fmaf(q.b1, xh1, xs[k]));
@@ -111,7 +110,7 @@ __device__ __forceinline__ void pass_aggregate(const IirParams& p, const float* 
             y1 = y;
         }
     }
-    float s0 = y2, s1 = y1;
+    float s0 = y2 * p.gain, s1 = y1 * p.gain;
     if (TPR == 2) {
         // row tail = A^(N/2) (first half's tail) + second half's zero-state tail
         const float t0 = __shfl_xor_sync(FULL_MASK, s0, 1);
@@ -236,7 +235,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
             if (lane == 0) {
                 if (bulk_of(c)) {
                     mbar_arrive_expect_tx(&aux->full[s], static_cast<uint32_t>(G::DATA_BYTES + G::HIST_BYTES));
-                    tma_load_2d(buf_of(s), &p.tmap_x, 0, static_cast<int>(c) * G::LINES, &aux->full[s]);
+                    tma_load_chunk<ROWS, N, IIR_TWO_PLANES>(buf_of(s), &p.tmap_x, c, &aux->full[s]);
                     tma_load_2d(hist_of(s), &p.tmap_h, 0, static_cast<int>(c) * G::LINES - 1, &aux->full[s]);
                 } else {
                     mbar_arrive(&aux->full[s]);  // element-wise chunk: the stage is free
@@ -254,7 +253,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
             const bool ok = pipe_wait(aux, &aux->done[s], spar(q), p, epoch);
             const bool stored = is_b && ok && bulk_of(c) && !*reinterpret_cast<volatile int*>(&aux->bail);
             if (lane == 0 && stored) {
-                tma_store_2d(&p.tmap_y, 0, static_cast<int>(c) * G::LINES, buf_of(s));
+                tma_store_chunk<ROWS, N, IIR_TWO_PLANES>(&p.tmap_y, c, buf_of(s));
                 bulk_commit();
             }
             if (q + S < items && ok) {
@@ -327,7 +326,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                 if (ok) {
                     for (int i = rt; i < G::CHUNK; i += NW * 32) {
                         const long long g = cs + i;
-                        b[swz<N>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
+                        b[swz<N, ROWS, IIR_TWO_PLANES>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
                     }
                     if (rt < 32) hist_of(s)[rt] = (cs - 32 + rt >= 0) ? p.x[cs - 32 + rt] : 0.f;
                 }
@@ -356,7 +355,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                     if (!*reinterpret_cast<volatile int*>(&aux->bail)) {
                         for (int i = rt; i < G::CHUNK; i += NW * 32) {
                             const long long g = cs + i;
-                            if (g < p.n) p.y[g] = b[swz<N>(i / N, i % N)];
+                            if (g < p.n) p.y[g] = b[swz<N, ROWS, IIR_TWO_PLANES>(i / N, i % N)];
                         }
                     }
                 }
