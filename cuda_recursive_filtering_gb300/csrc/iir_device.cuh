@@ -132,9 +132,16 @@ __device__ __forceinline__ uint32_t take_ticket(IirLaunchState* st, uint32_t nch
 
 // Short back-off between polls (about `cycles` / 2 ns, doubling up to a cap). The warp
 // sleeps rather than spins, so it takes no issue slots from the warps that compute.
+// Back-off between polls of a carry slot: a doubling sleep, capped at IIR_BACKOFF_CAP / 2 ns.
+// Every poll is an L2 round trip (several hundred ns) anyway; a short cap keeps the time between
+// a predecessor's publish and its observation close to that (measured at 2^28 samples, PH 32x64
+// orders 4 / 8 / 16: 609 / 389 / 221 GS/s with a 512 ns cap, 621 / 400 / 228 with 32 ns).
+#ifndef IIR_BACKOFF_CAP
+#define IIR_BACKOFF_CAP 64u
+#endif
 __device__ __forceinline__ void backoff(uint32_t& cycles) {
     __nanosleep(cycles >> 1);
-    if (cycles < 1024u) cycles <<= 1;
+    if (cycles < IIR_BACKOFF_CAP) cycles <<= 1;
 }
 
 // Barrier among the row warps only (named barrier 1; the control warp is not involved).
@@ -464,7 +471,7 @@ struct BlockGeom {
     static_assert(N == 16 || N == 32 || N == 64 || N == 128, "samples per row");
     static constexpr int CHUNK = ROWS * N;
     static constexpr int LINES = CHUNK / 32;          // 128-byte lines per chunk
-    static_assert(LINES <= 256, "one TMA box per chunk");
+    static_assert((N >= 32 ? ROWS : LINES) <= 256, "TMA box of at most 256 rows");
     static constexpr size_t DATA_BYTES = static_cast<size_t>(CHUNK) * sizeof(float);
     static constexpr size_t SMEM_BYTES = 1024 + DATA_BYTES + sizeof(BlockAux);  // + swizzle alignment
     // resident blocks per SM that shared memory (227 KB) and threads (2048) allow

@@ -360,13 +360,14 @@ int default_geometry(int kind, int n_sections, int& B, int& N) {
     return IIR_OK;
 }
 
-// Fastest realization by order, measured on GB300 at 2^28 samples: PH up to order 8 (700 / 483 /
-// 321 GS/s at orders 2 / 4 / 8; the precision form gives 310 at order 8); the precision form from
-// order 10, its cost nearly flat in the order while PH's grows with the sections (order 16: 279
-// against 190 GS/s, with a quarter of the error).
+// Fastest realization by order, measured on GB300 at 2^28 samples (butter(order, 0.05), N(0,1)
+// noise plus tones): PH up to order 12 (770 / 614 / 389 / 328 / 283 GS/s at orders 2 / 4 / 8 /
+// 10 / 12; the precision form gives 314 / 276 / 276 at orders 8 / 10 / 12); the precision form
+// from order 14, its cost nearly flat in the order while PH's grows with the sections (orders
+// 14 / 16: 279 / 284 against 248 / 221 GS/s, with a quarter of the error).
 int resolve_auto(int kernel, int n_sections) {
     if (kernel != IIR_KERNEL_AUTO) return kernel;
-    return n_sections >= 5 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
+    return n_sections >= 7 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
 }
 
 // samples per block (= per lookback unit)

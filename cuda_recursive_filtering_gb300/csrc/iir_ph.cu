@@ -41,6 +41,11 @@ static void add_ph_two(std::vector<KernelEntry>& reg) {
     reg.push_back(e);
 }
 
+// Rows per chunk of the one-block-per-chunk (cascade) kernel, per samples per row.
+#ifndef IIR_TICKET_ROWS_N64
+#define IIR_TICKET_ROWS_N64 128
+#endif
+
 void register_ph(std::vector<KernelEntry>& reg) {
     // single-section pipeline (chosen for one section when registered for the geometry)
     // (rows per chunk for 32, 64 and 128 samples per row: iir_pipe.cuh)
@@ -52,11 +57,11 @@ void register_ph(std::vector<KernelEntry>& reg) {
     add_ph_two<64, 128, IIR_PIPE_ROWS_N128>(reg);
     add_ph<32, 16, 128>(reg);
     add_ph<32, 32, 128>(reg);
-    add_ph<32, 64, 128>(reg);
+    add_ph<32, 64, IIR_TICKET_ROWS_N64>(reg);
     add_ph<32, 128, 64>(reg);
     add_ph<64, 16, 128>(reg);
     add_ph<64, 32, 128>(reg);
-    add_ph<64, 64, 128>(reg);
+    add_ph<64, 64, IIR_TICKET_ROWS_N64>(reg);
     add_ph<64, 128, 64>(reg);
 }
 
