@@ -486,10 +486,21 @@ int plan_create_plr(iir_plan** out, const double* b, const double* a, int order,
             phi[static_cast<size_t>(i) * k + j] = fac[static_cast<size_t>(j) * chunk + (chunk - k + i)];
     std::vector<float> tables(2 * 33 * static_cast<size_t>(k) * k);
     for (int i = 0; i < k; ++i) P[static_cast<size_t>(i) * k + i] = 1.0;
+    int depth = 0;  // least m <= 4 with ||Phi^m||_inf <= 1e-10 (truncated lookback), else 0
     for (int l = 0; l <= 32; ++l) {
         for (size_t q = 0; q < P.size(); ++q) tables[static_cast<size_t>(l) * k * k + q] = static_cast<float>(P[q]);
+        if (l >= 1 && l <= 4 && depth == 0) {
+            double norm = 0.0;
+            for (int i = 0; i < k; ++i) {
+                double row = 0.0;
+                for (int j = 0; j < k; ++j) row += std::fabs(P[static_cast<size_t>(i) * k + j]);
+                norm = std::max(norm, row);
+            }
+            if (std::isfinite(norm) && norm <= 1e-10) depth = l;
+        }
         matmul_k(P, phi, P, k);
     }
+    if (std::getenv("IIR_GB300_FULL_LOOKBACK")) depth = 0;
     phig = phi;  // Phi^32
     for (int sq = 0; sq < 5; ++sq) matmul_k(phig, phig, phig, k);
     Pg.assign(static_cast<size_t>(k) * k, 0.0);
@@ -518,6 +529,7 @@ int plan_create_plr(iir_plan** out, const double* b, const double* a, int order,
     q.pc = p->d_fac + facf.size();
     q.pg = q.pc + 33 * static_cast<size_t>(k) * k;
     q.chunk = chunk;
+    q.lb_depth = depth;
     q.gain = static_cast<float>(gain);
     for (int j = 0; j < order; ++j) {
         q.b[j] = static_cast<float>(b[j]);

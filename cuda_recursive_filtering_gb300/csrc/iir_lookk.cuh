@@ -61,6 +61,54 @@ __device__ __forceinline__ void warp_sumk(float (&v)[K]) {
     for (int i = 0; i < K; ++i) v[i] = warp_sum(v[i]);
 }
 
+// Truncated lookback (one full warp): when ||Phi^m|| <= 1e-10 (FP64, checked by the plan), the
+// incoming state of chunk c is X = sum_{i < min(m, c)} Phi^i part(c - 1 - i) (zero state before
+// the signal): lane i polls the part words of chunk c - 1 - i, and no chain of inclusive carries
+// is needed.
+template <int K, class P>
+__device__ bool lookback_trunc_k(const P& p, const unsigned long long* slots, const float* Pc, uint32_t c,
+                                 uint32_t epoch, int m, float (&X)[K]) {
+    constexpr int SW = 2 * K;
+    const int lane = threadIdx.x & 31;
+    const uint32_t pf = 2u * epoch + 1u;
+    const bool mine = lane < m && static_cast<uint32_t>(lane) < c;
+    float v[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) v[i] = 0.f;
+    const uint64_t t_start = globaltimer_ns();
+    uint32_t spin = 32;
+    while (true) {
+        bool ok = true;
+        if (mine) {
+            const unsigned long long* s = slots + static_cast<size_t>(c - 1 - lane) * SW;
+#pragma unroll
+            for (int i = 0; i < K; i += 2) {
+                unsigned long long a, b;
+                ld_relaxed_v2(s + i, a, b);
+                ok = ok && word_flag(a) == pf && word_flag(b) == pf;
+                v[i] = word_val(a);
+                v[i + 1] = word_val(b);
+            }
+        }
+        if (__all_sync(FULL_MASK, ok)) break;
+        int give_up = 0;
+        if (lane == 0) give_up = lookback_give_up(p, epoch, t_start) ? 1 : 0;
+        if (__shfl_sync(FULL_MASK, give_up, 0)) return false;
+        backoff(spin);
+    }
+    float t[K];
+    if (mine && lane > 0) {
+        matvec<K>(Pc + static_cast<size_t>(lane) * K * K, v, t);  // Phi^lane part(c - 1 - lane)
+    } else {
+#pragma unroll
+        for (int i = 0; i < K; ++i) t[i] = v[i];  // lane 0: Phi^0 = I (others: zero)
+    }
+    warp_sumk<K>(t);
+#pragma unroll
+    for (int i = 0; i < K; ++i) X[i] = t[i];
+    return true;
+}
+
 // One full warp. own = this chunk's part (needed for the group aggregate of a group's last chunk).
 template <int K, class P>
 __device__ bool lookback_hier_k(const P& p, unsigned long long* slots, unsigned long long* gslots,

@@ -97,6 +97,7 @@ struct IirPlrParams {
     unsigned int nchunks;
     unsigned int carry_cap;
     int chunk;                        // BLOCK * X
+    int lb_depth;                     // truncated lookback depth m (0: two-level lookback)
     float gain;
     float b[IIR_PLR_MAX_ORDER];       // FIR taps past b0 = 1
     float a[IIR_PLR_MAX_ORDER];       // recurrence taps: y[n] += a[j] y[n-j-1]

@@ -9,8 +9,10 @@
 //      a unit value in history slot j; plr_kernels.cuh:564-632);
 //   3. inter-warp doubling with the same factors through shared memory (plr_kernels.cuh:634-785);
 //   4. segment chaining over the X values per thread (plr_kernels.cuh:787-811);
-//   5. K-dimensional decoupled lookback for the chunk's incoming state (two-level, here) and the
-//      carry correction val += sum_j fac_j[i] X_j (plr_kernels.cuh:813-899).
+//   5. K-dimensional decoupled lookback for the chunk's incoming state and the carry correction
+//      val += sum_j fac_j[i] X_j (plr_kernels.cuh:813-899). The lookback is truncated to the m
+//      preceding chunks' aggregates when the chunk transition has decayed (||Phi^m|| <= 1e-10),
+//      else two-level over groups of 32 chunks.
 // Everything is float32 with plain products and sums, as in the reference, so order 16 keeps
 // its direct-form numerical fragility (reported by the accuracy tests, not hidden).
 #include "iir_lookk.cuh"
@@ -140,7 +142,9 @@ struct PlrBlock {
             unsigned long long* gslots = p.carry + static_cast<size_t>(p.carry_cap) * 2 * KO;
             if (lane == 0 && !withhold) publishk<KO>(slots + static_cast<size_t>(c) * 2 * KO, pf, own);
             bool ok = true;
-            if (c > 0) ok = lookback_hier_k<KO>(p, slots, gslots, p.pc, p.pg, c, epoch, own, withhold, Xc);
+            if (c > 0)
+                ok = p.lb_depth > 0 ? lookback_trunc_k<KO>(p, slots, p.pc, c, epoch, p.lb_depth, Xc)
+                                    : lookback_hier_k<KO>(p, slots, gslots, p.pc, p.pg, c, epoch, own, withhold, Xc);
             if (lane == 0) {
                 if (ok && !withhold) {
                     float f[KO];

@@ -239,6 +239,27 @@ def test_plr_from_filter_taps_hpp(order, cuda_device):
     assert oracle.errors(y, ref)["rel_max"] <= 1e-4
 
 
+@pytest.mark.parametrize("order,X", [(2, 8), (4, 8), (4, 1)])
+def test_plr_truncated_and_two_level_lookback(order, X, monkeypatch, cuda_device):
+    """PLR takes the truncated K-dimensional lookback when the chunk transition has decayed
+    (||Phi^m|| <= 1e-10, m <= 4) and the two-level lookback otherwise (IIR_GB300_FULL_LOOKBACK
+    forces it). Both meet the gate over hundreds of chunks and agree with each other."""
+    sos = butter(order)
+    bt = {2: 512, 4: 256}[order]
+    n = 300 * bt * X + 77
+    x = np.random.default_rng(order + X).uniform(-1, 1, n).astype(np.float32)
+    ref = golden(sos, x)
+    outs = []
+    for full in (False, True):
+        if full:
+            monkeypatch.setenv("IIR_GB300_FULL_LOOKBACK", "1")
+        y = run_plan(Plan(sos, "PLR", bt, X, max_n=n), x)
+        e = oracle.errors(y, ref)
+        assert e["finite"] and e["rel_max"] <= 1e-4, (full, e)
+        outs.append(y)
+    assert np.max(np.abs(outs[0] - outs[1])) <= 1e-5 * np.max(np.abs(ref))
+
+
 def test_plr_repeated_launches(cuda_device):
     sos = butter(4)
     plan = Plan(sos, "PLR", max_n=1 << 12)
