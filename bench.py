@@ -350,29 +350,33 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     achieved = BYTES_PER_SAMPLE * n / (ms * 1e-3) / 1e9
 
     # ---- end to end: host buffers through the public API (C ABI), copies inside ----
+    # iir_plan_execute_host: pinned host input and output; the copies of the signal's pieces
+    # overlap the filtering on three streams, each piece starting from the previous one's state.
     e2e = None
     if rank == 0 or world > 1:
         xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
         xh.copy_(x.cpu())
         yh = torch.empty(n, dtype=torch.float32, pin_memory=True)
-        xd = torch.empty_like(x)
-        yd = torch.empty_like(x)
+        hplan = Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=n)
         e2e_steps = max(2, min(args.steps, 5))
-        for _ in range(1):
-            xd.copy_(xh, non_blocking=True)
-            sosfilt(sos, xd, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], out=yd)
-            yh.copy_(yd, non_blocking=True)
-        torch.cuda.synchronize()
+        for _ in range(2):
+            hplan.filter_host(xh, out=yh)
+        hplan.check()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            xd.copy_(xh, non_blocking=True)
-            sosfilt(sos, xd, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], out=yd)
-            yh.copy_(yd, non_blocking=True)
+            hplan.filter_host(xh, out=yh)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / e2e_steps
+        hplan.check()
         e2e = {"value": world * n / dt / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n,
-               "ms_per_step": dt * 1e3}
-        del xh, yh, xd, yd
+               "ms_per_step": dt * 1e3, "api": "iir_plan_execute_host, pieces of 2^24 samples"}
+        if rank == 0:
+            yref = torch.empty(1 << 20, device=dev)
+            Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=1 << 20)(
+                x[:1 << 20], out=yref)
+            e2e["check_prefix_max_abs_diff"] = float((yh[:1 << 20].to(dev) - yref).abs().max())
+        hplan.close()
+        del xh, yh
 
     # ---- per-order / per-realization rows ----
     rows = {}

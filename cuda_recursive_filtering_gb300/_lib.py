@@ -65,6 +65,7 @@ def load(path: str | None = None):
         "iir_plan_create": ([pp, fp, i, i, i, i, sz], i),
         "iir_plan_create_plr_ba": ([pp, dp, dp, i, ctypes.c_double, i, i, sz], i),
         "iir_plan_execute": ([vp, vp, vp, sz, vp], i),
+        "iir_plan_execute_host": ([vp, vp, vp, sz, sz, vp], i),
         "iir_plan_check": ([vp, vp], i),
         "iir_plan_set_timeout_ns": ([vp, ll], i),
         "iir_plan_debug_withhold": ([vp, ll], i),

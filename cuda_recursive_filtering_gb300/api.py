@@ -103,6 +103,27 @@ class Plan:
         check(st, "iir_plan_execute")
         return out
 
+    def filter_host(self, x: torch.Tensor, out: torch.Tensor | None = None, piece: int = 0,
+                    stream=None) -> torch.Tensor:
+        """The filter over HOST float32 tensors (C ABI: iir_plan_execute_host). Pinned tensors
+        give overlapped copies; single-section plans on the two-pass schedule run in pieces
+        of ``piece`` samples (0 = 2^24), each starting from the state the previous left.
+        Stream-ordered: ``out`` is complete once ``stream`` (default: the current stream) is."""
+        for name, t in (("x", x), ("out", out)):
+            if t is None:
+                continue
+            if t.device.type != "cpu" or t.dtype != torch.float32 or not t.is_contiguous():
+                raise ValueError(f"{name} must be a contiguous float32 host tensor")
+        if out is None:
+            out = torch.empty(x.numel(), dtype=torch.float32, pin_memory=x.is_pinned())
+        if out.numel() != x.numel():
+            raise ValueError("out must have as many samples as x")
+        st = self._lib.iir_plan_execute_host(self._ptr, ctypes.c_void_p(x.data_ptr()),
+                                             ctypes.c_void_p(out.data_ptr()), x.numel(), int(piece),
+                                             _stream_handle(stream))
+        check(st, "iir_plan_execute_host")
+        return out
+
     def launches_per_execute(self) -> int:
         return int(self._lib.iir_plan_launches_per_execute(self._ptr))
 

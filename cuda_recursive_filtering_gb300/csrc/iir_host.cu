@@ -323,6 +323,35 @@ using namespace iirhost;
 // -------------------------------------------------------------------------------------------
 // plan
 // -------------------------------------------------------------------------------------------
+// Resources of iir_plan_execute_host, created on its first call: two slots of device input and
+// output buffers (piece samples each), the carried state, a copy stream per direction and the
+// events that order the three streams.
+struct HostStaging {
+    size_t cap = 0;               // samples per buffer
+    float* dx[2] = {nullptr, nullptr};
+    float* dy[2] = {nullptr, nullptr};
+    float* dz = nullptr;          // x[-2], x[-1], y[-2], y[-1] before the next piece
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t loaded[2] = {nullptr, nullptr};    // input slot filled
+    cudaEvent_t filtered[2] = {nullptr, nullptr};  // input slot read, output slot written
+    cudaEvent_t stored[2] = {nullptr, nullptr};    // output slot copied out
+};
+
+void host_staging_free(HostStaging* h) {
+    if (!h) return;
+    for (int b = 0; b < 2; ++b) {
+        if (h->dx[b]) cudaFree(h->dx[b]);
+        if (h->dy[b]) cudaFree(h->dy[b]);
+        if (h->loaded[b]) cudaEventDestroy(h->loaded[b]);
+        if (h->filtered[b]) cudaEventDestroy(h->filtered[b]);
+        if (h->stored[b]) cudaEventDestroy(h->stored[b]);
+    }
+    if (h->dz) cudaFree(h->dz);
+    if (h->h2d) cudaStreamDestroy(h->h2d);
+    if (h->d2h) cudaStreamDestroy(h->d2h);
+    delete h;
+}
+
 struct iir_plan {
     int device = 0;
     int kind = 0;
@@ -344,6 +373,7 @@ struct iir_plan {
     long long withhold = -1;
     unsigned long long launches = 0;  // since the carry slots were last zeroed
     size_t carry_bytes = 0;
+    HostStaging* host = nullptr;      // iir_plan_execute_host: device buffers, streams, events
 };
 
 namespace {
@@ -422,6 +452,10 @@ void plan_free(iir_plan* p) {
     if (p->tc) {
         p->d_state = nullptr;  // owned by the precision plan
         tc_plan_destroy(p->tc);
+    }
+    if (p->host) {
+        cudaDeviceSynchronize();
+        host_staging_free(p->host);
     }
     if (p->d_state) cudaFree(p->d_state);
     if (p->d_carry) cudaFree(p->d_carry);
@@ -653,14 +687,13 @@ int iir_plan_create_plr_ba(iir_plan** out, const double* b, const double* a, int
     return plan_create_plr(out, b, a, order, gain, block_size, values_per_thread, max_n);
 }
 
-int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stream_) {
-    if (!p || (n > 0 && (!x || !y))) return IIR_ERR_INVALID_ARGUMENT;
-    if (n == 0) return IIR_OK;
-    if (n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
-    const char* xb = reinterpret_cast<const char*>(x);
-    const char* yb = reinterpret_cast<const char*>(y);
-    if (xb < yb + n * sizeof(float) && yb < xb + n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;  // overlap
-    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+}  // extern "C"
+
+namespace {
+
+// One launch of the plan over device buffers (arguments checked by the caller). zi: initial
+// state of a single-section pipeline plan (x[-2], x[-1], y[-2], y[-1]), or null for rest.
+int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi, cudaStream_t stream) {
     if (p->kind == IIR_KIND_TC) {
         const int st = tc_plan_execute(p->tc, x, y, n, p->timeout_ns, p->withhold, stream);
         p->withhold = -1;
@@ -716,6 +749,7 @@ int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stre
                         : 0;
         q.timeout_ns = p->timeout_ns;
         q.withhold_chunk = p->withhold;
+        q.zi = p->entry->pipeline ? zi : nullptr;
         void* args[] = {&q};
         if (p->entry->pipeline) {
             // persistent: at most every resident block, all co-resident (cooperative launch)
@@ -728,6 +762,108 @@ int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stre
     }
     p->withhold = -1;  // one launch only
     return cuda_status(err);
+}
+
+// Device buffers, streams and events of iir_plan_execute_host for pieces of `cap` samples.
+int host_staging(iir_plan* p, size_t cap, HostStaging** out) {
+    HostStaging* h = p->host;
+    if (h && h->cap >= cap) {
+        *out = h;
+        return IIR_OK;
+    }
+    if (h) {
+        cudaDeviceSynchronize();
+        host_staging_free(h);
+        p->host = nullptr;
+    }
+    h = new HostStaging();
+    h->cap = cap;
+    int st = IIR_OK;
+    for (int b = 0; b < 2 && !st; ++b) {
+        st = cuda_status(cudaMalloc(&h->dx[b], cap * sizeof(float)));
+        if (!st) st = cuda_status(cudaMalloc(&h->dy[b], cap * sizeof(float)));
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->loaded[b], cudaEventDisableTiming));
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->filtered[b], cudaEventDisableTiming));
+        if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->stored[b], cudaEventDisableTiming));
+    }
+    if (!st) st = cuda_status(cudaMalloc(&h->dz, 4 * sizeof(float)));
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking));
+    if (!st) st = cuda_status(cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking));
+    if (st) {
+        host_staging_free(h);
+        return st;
+    }
+    p->host = h;
+    *out = h;
+    return IIR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int iir_plan_execute(iir_plan* p, const float* x, float* y, size_t n, void* stream_) {
+    if (!p || (n > 0 && (!x || !y))) return IIR_ERR_INVALID_ARGUMENT;
+    if (n == 0) return IIR_OK;
+    if (n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
+    const char* xb = reinterpret_cast<const char*>(x);
+    const char* yb = reinterpret_cast<const char*>(y);
+    if (xb < yb + n * sizeof(float) && yb < xb + n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;  // overlap
+    return plan_launch(p, x, y, n, nullptr, static_cast<cudaStream_t>(stream_));
+}
+
+int iir_plan_execute_host(iir_plan* p, const float* x, float* y, size_t n, size_t piece, void* stream_) {
+    if (!p || (n > 0 && (!x || !y))) return IIR_ERR_INVALID_ARGUMENT;
+    if (n == 0) return IIR_OK;
+    if (n > (1ull << 40)) return IIR_ERR_TOO_LARGE;
+    const char* xb = reinterpret_cast<const char*>(x);
+    const char* yb = reinterpret_cast<const char*>(y);
+    if (xb < yb + n * sizeof(float) && yb < xb + n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;  // overlap
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    // Pieces carry their state only on the single-section pipeline; other plans take one piece.
+    const bool carry = p->kind != IIR_KIND_PLR && p->kind != IIR_KIND_TC && p->entry && p->entry->pipeline;
+    if (piece == 0) piece = size_t(1) << 24;
+    piece = std::max<size_t>(piece, 1024);
+    if (!carry) piece = n;
+    piece = std::min(piece, n);
+    HostStaging* h = nullptr;
+    int st = host_staging(p, piece, &h);
+    if (st) return st;
+    // Work issued to the caller's stream before this call precedes the first copy.
+    cudaEvent_t start = nullptr;
+    st = cuda_status(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    if (!st) st = cuda_status(cudaEventRecord(start, stream));
+    if (!st) st = cuda_status(cudaStreamWaitEvent(h->h2d, start, 0));
+    if (start) cudaEventDestroy(start);
+    size_t i = 0;
+    for (size_t off = 0; off < n && !st; off += piece, ++i) {
+        const int b = static_cast<int>(i & 1);
+        const size_t len = std::min(piece, n - off);
+        // input slot b is free once the launch of piece i - 2 (and its state copies) has run
+        if (i >= 2) st = cuda_status(cudaStreamWaitEvent(h->h2d, h->filtered[b], 0));
+        if (!st) st = cuda_status(cudaMemcpyAsync(h->dx[b], x + off, len * sizeof(float), cudaMemcpyHostToDevice, h->h2d));
+        if (!st) st = cuda_status(cudaEventRecord(h->loaded[b], h->h2d));
+        // filter on the caller's stream once the input is in and the output slot is free
+        if (!st) st = cuda_status(cudaStreamWaitEvent(stream, h->loaded[b], 0));
+        if (!st && i >= 2) st = cuda_status(cudaStreamWaitEvent(stream, h->stored[b], 0));
+        if (!st) st = plan_launch(p, h->dx[b], h->dy[b], len, i > 0 ? h->dz : nullptr, stream);
+        if (!st && off + len < n) {
+            // state before the next piece: its last two inputs and outputs (len >= 1024 here)
+            st = cuda_status(cudaMemcpyAsync(h->dz, h->dx[b] + len - 2, 2 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                             stream));
+            if (!st)
+                st = cuda_status(cudaMemcpyAsync(h->dz + 2, h->dy[b] + len - 2, 2 * sizeof(float),
+                                                 cudaMemcpyDeviceToDevice, stream));
+        }
+        if (!st) st = cuda_status(cudaEventRecord(h->filtered[b], stream));
+        if (!st) st = cuda_status(cudaStreamWaitEvent(h->d2h, h->filtered[b], 0));
+        if (!st) st = cuda_status(cudaMemcpyAsync(y + off, h->dy[b], len * sizeof(float), cudaMemcpyDeviceToHost, h->d2h));
+        if (!st) st = cuda_status(cudaEventRecord(h->stored[b], h->d2h));
+    }
+    // the caller's stream completes after the last output copy
+    for (int b = 0; b < 2 && !st; ++b)
+        if (static_cast<size_t>(b) < i) st = cuda_status(cudaStreamWaitEvent(stream, h->stored[b], 0));
+    return st;
 }
 
 int iir_plan_check(iir_plan* p, void* stream_) {

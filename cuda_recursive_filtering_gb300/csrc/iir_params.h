@@ -66,6 +66,7 @@ struct IirParams {
     const float* x;
     float* y;
     long long n;
+    const float* zi;                  // single-section pipeline: initial state x[-2], x[-1], y[-2], y[-1] (or null)
     unsigned long long* carry;        // per section: [carry_cap][4] chunk slots, then group slots
     IirLaunchState* state;
     const float4* tables;             // [n_sections][IIR_TAB_STRIDE]

@@ -274,21 +274,23 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
         unsigned long long* gslots = slots + static_cast<size_t>(p.carry_cap) * 4;
         const float4 Q = tc[G::TC_QC + 1];
         const int lb_depth = static_cast<int>(p.tables[IIR_TAB_LBD].x);  // truncated lookback depth (0: two-level)
+        const float z0 = p.zi ? p.zi[2] : 0.f, z1 = p.zi ? p.zi[3] : 0.f;
         const uint32_t ff = 2u * epoch + 2u;
         bool failed = false;
         for (uint32_t k = 0; k < nk; ++k) {
             const int s = k % RING;
             const uint32_t c = chunk_of(k);
-            float X0 = 0.f, X1 = 0.f;
+            // chunk 0 starts from the signal's initial state (y[-2], y[-1]) (zero unless given)
+            float X0 = z0, X1 = z1;
             bool ok = pipe_wait(aux, &aux->part[s], rpar(k), p, epoch);
             ok = __all_sync(FULL_MASK, ok && !failed);  // warp-uniform: lookback_hier is a full-warp routine
             if (ok) {
                 const float a0 = aux->partv[s][0], a1 = aux->partv[s][1];
                 const bool withhold = static_cast<long long>(c) == p.withhold_chunk;
                 if (c > 0)
-                    ok = lb_depth > 0 ? lookback_trunc2(p, slots, tc + G::TC_QC, c, epoch, lb_depth, X0, X1)
+                    ok = lb_depth > 0 ? lookback_trunc2(p, slots, tc + G::TC_QC, c, epoch, lb_depth, X0, X1, z0, z1)
                                       : lookback_hier(p, slots, gslots, tc + G::TC_QC, tc + G::TC_QG, c, epoch, a0, a1,
-                                                      withhold, X0, X1);
+                                                      withhold, X0, X1, z0, z1);
                 if (lane == 0 && ok && !withhold) {
                     float q0, q1;
                     mv2(Q, X0, X1, q0, q1);
@@ -329,6 +331,15 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                         b[swz<N, ROWS, IIR_TWO_PLANES>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
                     }
                     if (rt < 32) hist_of(s)[rt] = (cs - 32 + rt >= 0) ? p.x[cs - 32 + rt] : 0.f;
+                }
+                named_barrier_rows(NW);
+            }
+            if (c == 0 && p.zi) {
+                // the two input samples before the signal come from the initial state
+                if (rt == 0) {
+                    hist_of(s)[30] = p.zi[0];
+                    hist_of(s)[31] = p.zi[1];
+                    fence_proxy_async_smem();  // before the stage is refilled by a tensor copy
                 }
                 named_barrier_rows(NW);
             }

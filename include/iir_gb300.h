@@ -114,6 +114,17 @@ int iir_plan_create_plr_ba(iir_plan** plan, const double* b, const double* a, in
 /* Launches the filter on x[0..n) -> y[0..n) on `stream` (stream-ordered, no sync). */
 int iir_plan_execute(iir_plan* plan, const float* x, float* y, size_t n, void* stream);
 
+/* The same filter over HOST buffers x[0..n) -> y[0..n) (pinned memory gives overlapped copies).
+ * Single-section plans on the two-pass schedule (order 2; PH, STCR, DTCR) run in pieces of
+ * `piece` samples (0 = 2^24): the input copy of the next piece, the filter of this piece and the
+ * output copy of the previous piece overlap on three streams, and each piece starts from the
+ * state the previous one left (its last two inputs and outputs). Other plans stage the whole
+ * signal. Stream-ordered: y is complete when `stream` has reached the end of this call. Device
+ * staging buffers are allocated on the first call (two pieces of input and of output). The
+ * reference's drivers copy the signal in, launch and copy out (src/test_accuracy.cu:116-159). */
+int iir_plan_execute_host(iir_plan* plan, const float* x, float* y, size_t n, size_t piece,
+                          void* stream);
+
 /* Synchronises `stream`, returns the first device-side error recorded by a launch of this
  * plan since the previous call (IIR_OK if none) and clears it. */
 int iir_plan_check(iir_plan* plan, void* stream);
