@@ -29,6 +29,7 @@
 // or the loop form (run-time loops over a thread-local array; the reference's *_LOOP
 // kernels). Both execute the same operations in the same order, so they are bit-identical.
 #pragma once
+#include <type_traits>
 #include "iir_device.cuh"
 #include "iir_twopass.cuh"
 
@@ -41,7 +42,9 @@ struct CrHalf {
     static_assert(L1 > 0, "half length");
 
     // Elimination level k (half-stride h), prev = previous row's kept tail before this level.
-    __device__ __forceinline__ static void eliminate(float (&u)[M], int h, float rk, float ek, float prev) {
+    // u: the half's values, in registers (register form) or in place in shared memory (loop form).
+    template <class U>
+    __device__ __forceinline__ static void eliminate(U&& u, int h, float rk, float ek, float prev) {
         float old = prev;  // level-(k-1) value of the previous group's kept position
 #pragma unroll(UNROLL ? 64 : 1)
         for (int g = 0; g < M; g += 2 * h) {
@@ -55,7 +58,8 @@ struct CrHalf {
     }
     // Back-substitution level k: ym1 = y at half position -1 (previous row's tail),
     // yfar = y at half position -1 - 2h (previous row's, or two rows back for h = M/2).
-    __device__ __forceinline__ static void backsub(float (&u)[M], int h, float ck, float dk, float ym1, float yfar) {
+    template <class U>
+    __device__ __forceinline__ static void backsub(U&& u, int h, float ck, float dk, float ym1, float yfar) {
 #pragma unroll(UNROLL ? 64 : 1)
         for (int g = 0; g < M; g += 2 * h) {
             const int d = g + h - 1;
@@ -73,6 +77,25 @@ struct CrHalf {
 namespace iirgb {
 
 constexpr int ilog2_c(int v) { return v <= 1 ? 0 : 1 + ilog2_c(v / 2); }
+
+// Loop-form storage: parity half p of row r, in place in the swizzled chunk buffer (half
+// index m is row position 2m + p). The loop forms index their halves with run-time loops; in
+// registers that would put the halves in local memory, so they work on the row itself.
+template <int N, int ROWS, bool PLANES>
+struct RowHalf {
+    float* buf;
+    int r, p;
+    __device__ __forceinline__ float& operator[](int m) const { return buf[swz<N, ROWS, PLANES>(r, 2 * m + p)]; }
+};
+// Both halves of a row (STCR), or this lane's half (DTCR: index 0 is parity p0).
+template <int N, int ROWS, bool PLANES, bool SPLIT>
+struct RowInPlace {
+    float* buf;
+    int r, p0;
+    __device__ __forceinline__ RowHalf<N, ROWS, PLANES> operator[](int hh) const {
+        return RowHalf<N, ROWS, PLANES>{buf, r, SPLIT ? p0 : hh};
+    }
+};
 
 // STCR (SPLIT = false): one thread per row holds both parity halves.
 // DTCR (SPLIT = true): the two halves of a row run on two neighbouring lanes (dim3(B, 2) in
@@ -115,6 +138,17 @@ struct CrBlock {
         if (ok) block_store<ROWS, N, THREADS>(p, buf, c);
     }
 
+    // Register-form storage of a row's halves (compile-time indices keep it in registers).
+    struct RegRow {
+        float v[NPAR][M];
+        __device__ __forceinline__ auto operator[](int hh) -> float (&)[M] { return v[hh]; }
+    };
+    // The row's storage for this form: registers, or the row in place in buf (loop form).
+    using Row = std::conditional_t<UNROLL, RegRow, RowInPlace<N, ROWS, PLANES, SPLIT>>;
+    __device__ __forceinline__ static void bind_row(Row& u, float* buf, int r, int p0) {
+        if constexpr (!UNROLL) u = Row{buf, r, p0};
+    }
+
     // previous row (same parity) of the tile, zero before the tile's first row
     __device__ __forceinline__ static float prev_row(float v, int rl) {
         const float o = __shfl_up_sync(FULL_MASK, v, TPR);
@@ -131,10 +165,13 @@ struct CrBlock {
     //     v[0] = y[0],  v[1] = y[1],  v[2] -= f_1 y[-2],  v[3] -= f_1 y[-1]
     // (y[0], y[1] from the section recurrence), after which the zero-padded solve returns the
     // true output of the tile.
+    // u: the row's halves, float[NPAR][M] in registers (register form) or RowInPlace (loop form:
+    // the solve overwrites the row in buf; every row thread of the block must call it, since it
+    // holds the row warps at a barrier until all rows have read their input history).
+    template <class UA>
     __device__ __forceinline__ static void solve_tile(const IirParams& p, const float* buf, const IirSection& q, int sec,
                                                       float h2, float h1, int r, int rl, int p0, float Xp0,
-                                                      float Xp1, float Y2, float Y1, float (&u)[NPAR][M], float& P0,
-                                                      float& P1) {
+                                                      float Xp1, float Y2, float Y1, UA&& u, float& P0, float& P1) {
         float s0[NPAR], s1[NPAR];
         // ---- FIR + first double-sided round -> u (own parity halves) ----
         const float g = (sec == 0) ? p.gain : 1.f;
@@ -158,19 +195,41 @@ struct CrBlock {
                         d4 = p0 ? c1 : c0, d5 = p0 ? c0 : 0.f;
             const float xm2 = m2, xm1 = m1;
             float xr0 = 0.f, xr1 = 0.f;  // raw x[0], x[1] of the row
+            if constexpr (UNROLL) {
 #pragma unroll
-            for (int j = 0; j < N / 4; ++j) {
-                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
-                if (j == 0) {
-                    xr0 = v4.x;
-                    xr1 = v4.y;
+                for (int j = 0; j < N / 4; ++j) {
+                    const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
+                    if (j == 0) {
+                        xr0 = v4.x;
+                        xr1 = v4.y;
+                    }
+                    u[0][2 * j] = fmaf(d5, v4.y, fmaf(d4, v4.x, fmaf(d3, m1, fmaf(d2, m2, fmaf(d1, m3, d0 * m4)))));
+                    u[0][2 * j + 1] =
+                        fmaf(d5, v4.w, fmaf(d4, v4.z, fmaf(d3, v4.y, fmaf(d2, v4.x, fmaf(d1, m1, d0 * m2)))));
+                    m4 = v4.x;
+                    m3 = v4.y;
+                    m2 = v4.z;
+                    m1 = v4.w;
                 }
-                u[0][2 * j] = fmaf(d5, v4.y, fmaf(d4, v4.x, fmaf(d3, m1, fmaf(d2, m2, fmaf(d1, m3, d0 * m4)))));
-                u[0][2 * j + 1] = fmaf(d5, v4.w, fmaf(d4, v4.z, fmaf(d3, v4.y, fmaf(d2, v4.x, fmaf(d1, m1, d0 * m2)))));
-                m4 = v4.x;
-                m3 = v4.y;
-                m2 = v4.z;
-                m1 = v4.w;
+            } else {
+                named_barrier_rows(NW);  // every row has read its input history before rows are overwritten
+#pragma unroll 1
+                for (int j = 0; j < N / 4; ++j) {
+                    const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
+                    if (j == 0) {
+                        xr0 = v4.x;
+                        xr1 = v4.y;
+                    }
+                    const float o0 = fmaf(d5, v4.y, fmaf(d4, v4.x, fmaf(d3, m1, fmaf(d2, m2, fmaf(d1, m3, d0 * m4)))));
+                    const float o1 = fmaf(d5, v4.w, fmaf(d4, v4.z, fmaf(d3, v4.y, fmaf(d2, v4.x, fmaf(d1, m1, d0 * m2)))));
+                    m4 = v4.x;
+                    m3 = v4.y;
+                    m2 = v4.z;
+                    m1 = v4.w;
+                    __syncwarp();  // both lanes of the row have read these four samples
+                    u[0][2 * j] = o0;
+                    u[0][2 * j + 1] = o1;
+                }
             }
             if (rl == 0) {
                 // first row of the tile: y[0] = w[0] + a1 y[-1] + a2 y[-2], y[1] = w[1] + a1 y[0] + a2 y[-1]
@@ -203,19 +262,40 @@ struct CrBlock {
             // w[-2], w[-1]: zero before the tile (zero-padded system), else the FIR
             float w2 = (rl > 0) ? fmaf(b2, x4, fmaf(b1, x3, x2)) : 0.f;
             float w1 = (rl > 0) ? fmaf(b2, x3, fmaf(b1, x2, x1)) : 0.f;
+            if constexpr (UNROLL) {
 #pragma unroll
-            for (int j = 0; j < N / 4; ++j) {
-                const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
-                const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
+                for (int j = 0; j < N / 4; ++j) {
+                    const float4 v4 = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, PLANES>(r, 4 * j));
+                    const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int n = 4 * j + k;
-                    const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
-                    u[n & 1][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
-                    x2 = x1;
-                    x1 = xs[k];
-                    w2 = w1;
-                    w1 = wn;
+                    for (int k = 0; k < 4; ++k) {
+                        const int n = 4 * j + k;
+                        const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
+                        u[n & 1][n >> 1] = fmaf(f, w2, fmaf(-e, w1, wn));
+                        x2 = x1;
+                        x1 = xs[k];
+                        w2 = w1;
+                        w1 = wn;
+                    }
+                }
+            } else {
+                named_barrier_rows(NW);  // every row has read its input history before rows are overwritten
+#pragma unroll 1
+                for (int j = 0; j < N / 4; ++j) {
+                    float4* ptr = reinterpret_cast<float4*>(u[0].buf + swz<N, ROWS, PLANES>(r, 4 * j));
+                    const float4 v4 = *ptr;
+                    const float xs[4] = {v4.x * g, v4.y * g, v4.z * g, v4.w * g};
+                    float o[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float wn = fmaf(b2, x2, fmaf(b1, x1, xs[k]));
+                        o[k] = fmaf(f, w2, fmaf(-e, w1, wn));  // row position 4j + k (half k & 1)
+                        x2 = x1;
+                        x1 = xs[k];
+                        w2 = w1;
+                        w1 = wn;
+                    }
+                    *ptr = make_float4(o[0], o[1], o[2], o[3]);
                 }
             }
             if (rl == 0) {
@@ -271,8 +351,8 @@ struct CrBlock {
 
     // u += response of the section recurrence to the row's incoming pair (d2, d1) =
     // (delta[-2], delta[-1]). DTCR: each parity runs the stride-2 recurrence of its half.
-    __device__ __forceinline__ static void add_response(float (&u)[NPAR][M], const IirSection& q, int p0, float d2,
-                                                        float d1) {
+    template <class UA>
+    __device__ __forceinline__ static void add_response(UA&& u, const IirSection& q, int p0, float d2, float d1) {
         const float a1 = q.a1, a2 = q.a2;
         if (SPLIT) {
             // stride-2 recurrence of this parity: delta[2m+p] from (delta[p], delta[p+2])
@@ -303,8 +383,10 @@ struct CrBlock {
     }
 
     // Row r from this thread's halves into the swizzled buffer (DTCR: each lane stores its own
-    // parity's samples).
-    __device__ __forceinline__ static void write_row(float* buf, const float (&u)[NPAR][M], int r, int p0) {
+    // parity's samples). The loop form has solved the row in place: nothing to write.
+    template <class UA>
+    __device__ __forceinline__ static void write_row(float* buf, UA&& u, int r, int p0) {
+        if constexpr (!UNROLL) return;
         if (SPLIT) {
             // The row's lane pair holds the even (p0 = 0) and odd (p0 = 1) samples. Float4 j is
             // (e[2j], o[2j], e[2j+1], o[2j+1]); the even lane stores the even j, the odd lane the
@@ -336,7 +418,8 @@ struct CrBlock {
         const int rl = SPLIT ? (lane >> 1) : lane;  // row within the tile (warp)
         const int r = w * RW + rl;                    // row within the chunk
         const int p0 = SPLIT ? (lane & 1) : 0;        // first parity handled
-        float u[NPAR][M];
+        typename CrBlock::Row u;  // (register form: written by the first solve before any read)
+        bind_row(u, buf, r, p0);
         float Xp0 = 0.f, Xp1 = 0.f;  // previous section's incoming state (row-0 input history)
         float h2 = 0.f, h1 = 0.f;    // input samples before the chunk
         if (row_warp && r == 0 && c > 0) {
@@ -414,7 +497,8 @@ struct CrTwo {
             S0 = t0 + zin[RW * w][0];
             S1 = t1 + zin[RW * w][1];
         }
-        float u[NPAR][M];
+        typename Blk::Row u;
+        Blk::bind_row(u, buf, r, p0);
         float P0, P1;
         Blk::solve_tile(p, buf, q, 0, hist[30], hist[31], r, rl, p0, 0.f, 0.f, S0, S1, u, P0, P1);
         named_barrier_rows(NW);  // every row has read its input history
