@@ -218,7 +218,7 @@ def run_batching(dev) -> dict:
     from cuda_recursive_filtering_gb300 import Batch, workloads
 
     filters, lens = workloads.multichannel_mixed()
-    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 4096 + len(filters)), device=dev)
+    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 8192 + len(filters)), device=dev)
     off = np.concatenate([[0], np.cumsum(lens)])
     x = workloads.uniform_signal(int(off[-1]), 3, device=dev)
     y = torch.empty_like(x)

@@ -198,7 +198,7 @@ class Batch:
     list of segments ``(x, y, filter_index, zi, zf)``: CUDA float32 tensors for input and
     output, the filter's index, and optional device state in / out tensors of
     ``state_size(filter)`` floats (None = start at rest / do not report). Segments are filtered
-    independently (PH solve; chunks of 4096 samples; the lookback stays inside a segment).
+    independently (PH solve; chunks of 8192 samples; the lookback stays inside a segment).
     State layout: x[-2], x[-1] of the raw input, then each section's y[-2], y[-1].
     """
 

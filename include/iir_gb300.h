@@ -170,7 +170,7 @@ typedef struct iir_batch iir_batch;
  * (sum of n_sections[f] rows of 6), n_sections[f] in 1..8. Capacities grow on demand. */
 int iir_batch_create(iir_batch** batch, const float* sos, const int* n_sections, int n_filters,
                      size_t max_segments, size_t max_chunks);
-/* Filters every segment in one launch on `stream` (PH solve, chunks of 4096 samples, the
+/* Filters every segment in one launch on `stream` (PH solve, chunks of 8192 samples, the
  * decoupled lookback restricted to each segment). Stream-ordered; launches of one batch
  * plan must be ordered on one stream at a time. */
 int iir_batch_execute(iir_batch* batch, const iir_segment* segs, int n_segs, void* stream);
