@@ -134,13 +134,32 @@ struct BatchBlock {
                 if (i < V) *reinterpret_cast<float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N)) = v[k];
             }
         } else {
-            for (int i = tid; i < CHUNK; i += THREADS) buf[swz<N, ROWS, true>(i / N, i % N)] = (i < nrem) ? sg.x[cs + i] : 0.f;
+            // unaligned or partial chunk: coalesced scalar loads, a batch of them in flight per
+            // thread before the stores (zero past the segment's end)
+            constexpr int PS = (CHUNK + THREADS - 1) / THREADS, BT = 8;
+            for (int k0 = 0; k0 < PS; k0 += BT) {
+                float t[BT];
+#pragma unroll
+                for (int k = 0; k < BT; ++k) {
+                    const int i = tid + (k0 + k) * THREADS;
+                    t[k] = (i < CHUNK && i < nrem) ? __ldg(sg.x + cs + i) : 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < BT; ++k) {
+                    const int i = tid + (k0 + k) * THREADS;
+                    if (i < CHUNK) buf[swz<N, ROWS, true>(i / N, i % N)] = t[k];
+                }
+            }
         }
         __syncthreads();
 
         const bool row_warp = warp > 0;
         const int w = warp - 1;
         const int r = w * 32 + lane;
+        // A row warp whose rows all lie past the segment's end (padding of its last chunk) only
+        // takes part in the barriers: nothing there is stored, and the chunk's aggregate (the
+        // segment's last) has no reader.
+        const bool live = row_warp && static_cast<long long>(w) * 32 * N < nrem;
         const float gain = flt.gain;
         float xh2 = 0.f, xh1 = 0.f;
         if (row_warp) {
@@ -157,7 +176,7 @@ struct BatchBlock {
             xh2 *= gain;
             xh1 *= gain;
             named_barrier_rows(NW);
-            if (gain != 1.f) {
+            if (live && gain != 1.f) {
 #pragma unroll 4
                 for (int j = 0; j < N / 4; ++j) {
                     float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
@@ -174,19 +193,19 @@ struct BatchBlock {
             const float4* tab = p.tables + static_cast<size_t>(flt.sec0 + sec) * IIR_BT_STRIDE;
             const float4 Gw = tab[IIR_BT_GPOW + 31];
             float s0 = 0.f, s1 = 0.f, in0 = 0.f, in1 = 0.f;
-            if (row_warp) {
+            if (live) {
                 if (sec == 0)
                     Ph::template filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1);
                 else
                     Ph::template filter_pass<true>(buf, r, q.b1, q.b2, q.a1, q.a2, pa1, pa2, d2, d1, xh2, xh1, s0, s1);
                 warp_scan2<32, 1>(s0, s1, q.M, lane);
-                if (lane == 31) {
-                    aux->wtot[w][0][0] = s0;
-                    aux->wtot[w][0][1] = s1;
-                }
+            }
+            if (row_warp && lane == 31) {
+                aux->wtot[w][0][0] = s0;
+                aux->wtot[w][0][1] = s1;
             }
             __syncthreads();  // (A)
-            if (row_warp) {
+            if (live) {
                 warp_incoming(aux, w, 0, Gw, in0, in1);
                 if (w > 0) {
                     float e0, e1;
@@ -194,12 +213,12 @@ struct BatchBlock {
                     s0 += e0;
                     s1 += e1;
                 }
-            } else {
+            } else if (!row_warp) {
                 control(p, aux, sg, sec, lc, epoch, tab, Gw);
             }
             __syncthreads();  // (B)
             if (aux->bail) return;
-            if (row_warp) {
+            if (live) {
                 const float X0 = aux->X[0], X1 = aux->X[1];
                 float P0, P1;
                 mv2(tab[IIR_BT_CPOW + r], X0, X1, P0, P1);
@@ -245,7 +264,7 @@ struct BatchBlock {
                 xh1 = i1;
             }
         }
-        if (row_warp) Ph::correct_pass(buf, r, pa1, pa2, d2, d1);
+        if (live) Ph::correct_pass(buf, r, pa1, pa2, d2, d1);
         __syncthreads();
         const long long cnt = nrem < CHUNK ? nrem : CHUNK;
         if (cnt == CHUNK && (reinterpret_cast<uintptr_t>(sg.y) & 15u) == 0) {
