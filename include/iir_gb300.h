@@ -120,8 +120,9 @@ int iir_plan_execute(iir_plan* plan, const float* x, float* y, size_t n, void* s
  * output copy of the previous piece overlap on three streams, and each piece starts from the
  * state the previous one left (its last two inputs and outputs). Other plans stage the whole
  * signal. Stream-ordered: y is complete when `stream` has reached the end of this call. Device
- * staging buffers are allocated on the first call (two pieces of input and of output). The
- * reference's drivers copy the signal in, launch and copy out (src/test_accuracy.cu:116-159). */
+ * staging buffers, two copy streams and events are created on the first call (two pieces of
+ * input and of output); a call is not meant for stream capture. The reference's drivers copy
+ * the signal in, launch and copy out (src/test_accuracy.cu:116-159). */
 int iir_plan_execute_host(iir_plan* plan, const float* x, float* y, size_t n, size_t piece,
                           void* stream);
 
