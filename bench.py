@@ -32,8 +32,10 @@ METRIC = "GS/s (fp32 samples per second through the cascaded-biquad filter)"
 UNIT = "GS/s"
 LOG2N = 28
 HEADLINE = {"kernel": "DTCR_UNROLL", "order": 2, "block_size": 32, "n_blocks": 64}
-SWEEP_GEOM = {"PH": [(32, 32), (32, 64)], "STCR": [(32, 32), (32, 64)], "STCR_UNROLL": [(32, 32), (32, 64)],
-              "DTCR": [(32, 32), (32, 64)], "DTCR_UNROLL": [(32, 32), (32, 64)], "PLR": [(0, 0)]}
+# the reference's geometry set BLOCK_SIZE x N_BLOCKS (stcr_kernels.cuh:3613-3624)
+_GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
+SWEEP_GEOM = {"PH": _GEOMS, "STCR": _GEOMS, "STCR_UNROLL": _GEOMS, "DTCR": _GEOMS, "DTCR_UNROLL": _GEOMS,
+              "PLR": [(0, 0)]}
 BYTES_PER_SAMPLE = 8  # 4 read + 4 written (algorithmic)
 
 
