@@ -480,7 +480,7 @@ struct CrBlock {
 // writes once (no tile join, no response added afterwards).
 template <bool SPLIT, int N_, int ROWS_, bool UNROLL>
 struct CrTwo {
-    using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL, IIR_TWO_PLANES>;
+    using Blk = CrBlock<SPLIT, 32, N_, ROWS_, UNROLL, two_planes(N_)>;
     static constexpr int N = N_, ROWS = ROWS_, M = Blk::M, NPAR = Blk::NPAR, RW = Blk::RW, NW = Blk::NW;
     static constexpr int TPR = Blk::TPR;
 

@@ -37,7 +37,7 @@ static void add_ph_two(std::vector<KernelEntry>& reg) {
     KernelEntry e{IIR_KIND_PH, B, N, (const void*)iir_ph_two_kernel<N, ROWS, IIR_TWO_STAGES, IIR_TWO_LAG>, 64 + ROWS,
                   TwoPassGeom<ROWS, N, IIR_TWO_STAGES, IIR_TWO_LAG>::SMEM_BYTES, 0, ROWS};
     e.pipeline = 1;
-    e.planes = IIR_TWO_PLANES;
+    e.planes = two_planes(N) ? 1 : 0;
     reg.push_back(e);
 }
 

@@ -213,8 +213,8 @@ struct PhTwo {
         const float gain = p.gain;
         float xh2, xh1;
         if (r > 0) {
-            xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 2)];
-            xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 1)];
+            xh2 = buf[swz<N, ROWS, two_planes(N)>(r - 1, N - 2)];
+            xh1 = buf[swz<N, ROWS, two_planes(N)>(r - 1, N - 1)];
         } else {
             xh2 = hist[30];
             xh1 = hist[31];
@@ -231,7 +231,7 @@ struct PhTwo {
         named_barrier_rows(NW);  // every row has its input history before rows are overwritten
 #pragma unroll 4
         for (int j = 0; j < N / 4; ++j) {
-            float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, IIR_TWO_PLANES>(r, 4 * j));
+            float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, two_planes(N)>(r, 4 * j));
             const float4 v = *ptr;
             const float xs[4] = {v.x * gain, v.y * gain, v.z * gain, v.w * gain};
             float ys[4];

@@ -19,9 +19,18 @@ namespace iirgb {
 
 // Shared-memory layout of the single-section pipelines' chunk buffers (swz in iir_device.cuh):
 // 0 = lines (one tensor copy per chunk, contiguous in memory), 1 = planes of 32-sample columns.
+// Measured at 2^28 samples, order 2: rows of 64 samples keep lines (planes cost 5-7%: each
+// plane copy reads 128 of every 256 bytes); rows of 128 samples take planes, since lines leave
+// them 4-way bank conflicts (32x128: PH 530 -> 688, STCR_UNROLL 477 -> 650, DTCR_UNROLL
+// 625 -> 725 GS/s).
 #ifndef IIR_TWO_PLANES
 #define IIR_TWO_PLANES 0
 #endif
+#ifndef IIR_TWO_PLANES_N128
+#define IIR_TWO_PLANES_N128 1
+#endif
+// Layout of a single-section pipeline's chunk buffer for rows of N samples.
+constexpr bool two_planes(int n) { return n >= 128 ? (IIR_TWO_PLANES_N128 != 0) : (IIR_TWO_PLANES != 0); }
 
 struct PipeAux {
     unsigned long long full[8];

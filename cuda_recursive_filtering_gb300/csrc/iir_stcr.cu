@@ -49,7 +49,7 @@ static void add_two(std::vector<KernelEntry>& reg) {
         KernelEntry e{kind, b, N, (const void*)iir_stcr_two_kernel<N, ROWS, UNROLL, IIR_TWO_STAGES, IIR_TWO_LAG>,
                       64 + R::NW * 32, TwoPassGeom<ROWS, N, IIR_TWO_STAGES, IIR_TWO_LAG>::SMEM_BYTES, 0, ROWS};
         e.pipeline = 1;
-        e.planes = IIR_TWO_PLANES;
+        e.planes = two_planes(N) ? 1 : 0;
         reg.push_back(e);
     }
 }

@@ -84,11 +84,11 @@ __device__ __forceinline__ void pass_aggregate(const IirParams& p, const float* 
     const IirSection& q = p.sec[0];
     float xh2, xh1;
     if (n0 > 0) {
-        xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r, n0 - 2)];
-        xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r, n0 - 1)];
+        xh2 = buf[swz<N, ROWS, two_planes(N)>(r, n0 - 2)];
+        xh1 = buf[swz<N, ROWS, two_planes(N)>(r, n0 - 1)];
     } else if (r > 0) {
-        xh2 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 2)];
-        xh1 = buf[swz<N, ROWS, IIR_TWO_PLANES>(r - 1, N - 1)];
+        xh2 = buf[swz<N, ROWS, two_planes(N)>(r - 1, N - 2)];
+        xh1 = buf[swz<N, ROWS, two_planes(N)>(r - 1, N - 1)];
     } else {
         xh2 = hist[30];
         xh1 = hist[31];
@@ -98,7 +98,7 @@ __device__ __forceinline__ void pass_aggregate(const IirParams& p, const float* 
     float y1 = 0.f, y2 = 0.f;
 #pragma unroll 4
     for (int j = 0; j < SPAN / 4; ++j) {
-        const float4 v = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, IIR_TWO_PLANES>(r, n0 + 4 * j));
+        const float4 v = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, two_planes(N)>(r, n0 + 4 * j));
         const float xs[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -235,7 +235,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
             if (lane == 0) {
                 if (bulk_of(c)) {
                     mbar_arrive_expect_tx(&aux->full[s], static_cast<uint32_t>(G::DATA_BYTES + G::HIST_BYTES));
-                    tma_load_chunk<ROWS, N, IIR_TWO_PLANES>(buf_of(s), &p.tmap_x, c, &aux->full[s]);
+                    tma_load_chunk<ROWS, N, two_planes(N)>(buf_of(s), &p.tmap_x, c, &aux->full[s]);
                     tma_load_2d(hist_of(s), &p.tmap_h, 0, static_cast<int>(c) * G::LINES - 1, &aux->full[s]);
                 } else {
                     mbar_arrive(&aux->full[s]);  // element-wise chunk: the stage is free
@@ -253,7 +253,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
             const bool ok = pipe_wait(aux, &aux->done[s], spar(q), p, epoch);
             const bool stored = is_b && ok && bulk_of(c) && !*reinterpret_cast<volatile int*>(&aux->bail);
             if (lane == 0 && stored) {
-                tma_store_chunk<ROWS, N, IIR_TWO_PLANES>(&p.tmap_y, c, buf_of(s));
+                tma_store_chunk<ROWS, N, two_planes(N)>(&p.tmap_y, c, buf_of(s));
                 bulk_commit();
             }
             if (q + S < items && ok) {
@@ -328,7 +328,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                 if (ok) {
                     for (int i = rt; i < G::CHUNK; i += NW * 32) {
                         const long long g = cs + i;
-                        b[swz<N, ROWS, IIR_TWO_PLANES>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
+                        b[swz<N, ROWS, two_planes(N)>(i / N, i % N)] = (g < p.n) ? p.x[g] : 0.f;
                     }
                     if (rt < 32) hist_of(s)[rt] = (cs - 32 + rt >= 0) ? p.x[cs - 32 + rt] : 0.f;
                 }
@@ -366,7 +366,7 @@ __device__ __forceinline__ void run_twopass(const IirParams& p, unsigned char* s
                     if (!*reinterpret_cast<volatile int*>(&aux->bail)) {
                         for (int i = rt; i < G::CHUNK; i += NW * 32) {
                             const long long g = cs + i;
-                            if (g < p.n) p.y[g] = b[swz<N, ROWS, IIR_TWO_PLANES>(i / N, i % N)];
+                            if (g < p.n) p.y[g] = b[swz<N, ROWS, two_planes(N)>(i / N, i % N)];
                         }
                     }
                 }
