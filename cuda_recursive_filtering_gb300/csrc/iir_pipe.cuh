@@ -6,9 +6,15 @@
 
 namespace iirgb {
 
-// Rows per chunk of the single-section pipelines, per samples per row (chunks of 8192 samples).
+// Rows per chunk of the single-section pipelines, per samples per row: chunks of 8192 samples,
+// except rows of 32 samples for PH and DTCR (128 rows, 4096 samples). Measured at 2^28, order 2,
+// 32x32, 256 -> 128 rows: PH 715 -> 769, DTCR_UNROLL 480 -> 512, STCR_UNROLL 719 -> 706 GS/s, so
+// STCR keeps 256.
 #ifndef IIR_PIPE_ROWS_N32
-#define IIR_PIPE_ROWS_N32 256
+#define IIR_PIPE_ROWS_N32 128
+#endif
+#ifndef IIR_PIPE_ROWS_N32_STCR
+#define IIR_PIPE_ROWS_N32_STCR 256
 #endif
 #ifndef IIR_PIPE_ROWS_N64
 #define IIR_PIPE_ROWS_N64 128

@@ -56,8 +56,8 @@ static void add_two(std::vector<KernelEntry>& reg) {
 
 void register_stcr(std::vector<KernelEntry>& reg) {
     // rows per chunk for 32, 64 and 128 samples per row: iir_pipe.cuh
-    add_two<32, IIR_PIPE_ROWS_N32, true>(reg);
-    add_two<32, IIR_PIPE_ROWS_N32, false>(reg);
+    add_two<32, IIR_PIPE_ROWS_N32_STCR, true>(reg);
+    add_two<32, IIR_PIPE_ROWS_N32_STCR, false>(reg);
     add_two<64, IIR_PIPE_ROWS_N64, true>(reg);
     add_two<64, IIR_PIPE_ROWS_N64, false>(reg);
     add_two<128, IIR_PIPE_ROWS_N128, true>(reg);
