@@ -282,23 +282,32 @@ def run_precision(dev, log2n: int) -> dict:
     return out
 
 
-def run_serving(dev, seconds: float = 6.0) -> dict:
+def run_serving(dev, seconds: float = 4.0, runs: int = 3) -> dict:
     """Continuous-batching stream server under Poisson arrivals (host chunks in, results back
-    on the host): achieved GS/s and request latency percentiles."""
+    on the host): achieved GS/s and request latency percentiles. The load runs ``runs`` times;
+    the top-level figures are the run with the median p99, and every run is listed (a rare
+    host-side stall of tens to hundreds of milliseconds sets the p99 of the run it falls in)."""
     from cuda_recursive_filtering_gb300 import workloads
     from cuda_recursive_filtering_gb300.serving import StreamServer, run_poisson_load
 
     filters, load = workloads.streaming_poisson()
     srv = StreamServer(filters, max_batch=1024, max_streams=len(filters), device=dev, keep_outputs=False)
     streams = [srv.open_stream(i) for i in range(len(filters))]
-    run_poisson_load(srv, streams, rate_sps=load["rate_sps"] / 4, duration_s=0.3, chunk_lo=load["chunk_lo"],
-                     chunk_hi=load["chunk_hi"], seed=1)  # warm-up
-    srv.completed.clear()
-    srv.samples_done = 0
-    out = run_poisson_load(srv, streams, rate_sps=load["rate_sps"], duration_s=seconds, chunk_lo=load["chunk_lo"],
-                           chunk_hi=load["chunk_hi"], seed=load["seed"])
+    # warm-up at the full rate, so that the first measured run finds every buffer at its working size
+    run_poisson_load(srv, streams, rate_sps=load["rate_sps"], duration_s=1.0, chunk_lo=load["chunk_lo"],
+                     chunk_hi=load["chunk_hi"], seed=1)
+    results = []
+    for k in range(runs):
+        srv.completed.clear()
+        srv.samples_done = 0
+        results.append(run_poisson_load(srv, streams, rate_sps=load["rate_sps"], duration_s=seconds,
+                                        chunk_lo=load["chunk_lo"], chunk_hi=load["chunk_hi"], seed=load["seed"] + k))
+    order = sorted(range(runs), key=lambda i: results[i]["p99_us"] or 0.0)
+    out = dict(results[order[runs // 2]])
+    out["runs"] = [{k: round(r[k], 3) for k in ("gsps", "p50_us", "p99_us", "max_us")} for r in results]
     out["workload"] = ("1024 streams, order-8 butter cutoff U[0.05, 0.4] each; chunks U[256, 65536]; "
-                       f"Poisson arrivals {load['rate_sps']:.0e} samples/s; {seconds:g} s; host chunks in and out")
+                       f"Poisson arrivals {load['rate_sps']:.0e} samples/s; {runs} runs of {seconds:g} s "
+                       "(top level: the run with the median p99); host chunks in and out")
     return out
 
 
