@@ -79,6 +79,7 @@ def test_status_strings_and_argument_checks(built_library):
     assert L.iir_plan_create(ctypes.byref(p), None, 1, 1, 32, 64, 1024) == _lib.IIR_ERR_INVALID_ARGUMENT
     assert L.iir_plan_create(ctypes.byref(p), sos, 1, 99, 32, 64, 1024) == _lib.IIR_ERR_INVALID_ARGUMENT
     assert L.iir_plan_execute(None, None, None, 16, None) == _lib.IIR_ERR_INVALID_ARGUMENT
+    assert L.iir_plan_execute_host(None, None, None, 16, 0, None) == _lib.IIR_ERR_INVALID_ARGUMENT
     assert L.iir_plan_destroy(None) == _lib.IIR_ERR_INVALID_ARGUMENT
 
 
