@@ -328,6 +328,7 @@ using namespace iirhost;
 // events that order the three streams.
 struct HostStaging {
     size_t cap = 0;               // samples per buffer
+    int slots = 0;                // 2 (pieces in flight) or 1 (the whole signal in one piece)
     float* dx[2] = {nullptr, nullptr};
     float* dy[2] = {nullptr, nullptr};
     float* dz = nullptr;          // x[-2], x[-1], y[-2], y[-1] before the next piece
@@ -335,6 +336,7 @@ struct HostStaging {
     cudaEvent_t loaded[2] = {nullptr, nullptr};    // input slot filled
     cudaEvent_t filtered[2] = {nullptr, nullptr};  // input slot read, output slot written
     cudaEvent_t stored[2] = {nullptr, nullptr};    // output slot copied out
+    cudaEvent_t start = nullptr;                   // caller's stream at the call
 };
 
 void host_staging_free(HostStaging* h) {
@@ -347,6 +349,7 @@ void host_staging_free(HostStaging* h) {
         if (h->stored[b]) cudaEventDestroy(h->stored[b]);
     }
     if (h->dz) cudaFree(h->dz);
+    if (h->start) cudaEventDestroy(h->start);
     if (h->h2d) cudaStreamDestroy(h->h2d);
     if (h->d2h) cudaStreamDestroy(h->d2h);
     delete h;
@@ -764,10 +767,11 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
     return cuda_status(err);
 }
 
-// Device buffers, streams and events of iir_plan_execute_host for pieces of `cap` samples.
-int host_staging(iir_plan* p, size_t cap, HostStaging** out) {
+// Device buffers, streams and events of iir_plan_execute_host: `slots` input and output buffers of
+// `cap` samples each.
+int host_staging(iir_plan* p, size_t cap, int slots, HostStaging** out) {
     HostStaging* h = p->host;
-    if (h && h->cap >= cap) {
+    if (h && h->cap >= cap && h->slots >= slots) {
         *out = h;
         return IIR_OK;
     }
@@ -778,15 +782,17 @@ int host_staging(iir_plan* p, size_t cap, HostStaging** out) {
     }
     h = new HostStaging();
     h->cap = cap;
+    h->slots = slots;
     int st = IIR_OK;
     for (int b = 0; b < 2 && !st; ++b) {
-        st = cuda_status(cudaMalloc(&h->dx[b], cap * sizeof(float)));
-        if (!st) st = cuda_status(cudaMalloc(&h->dy[b], cap * sizeof(float)));
+        if (b < slots) st = cuda_status(cudaMalloc(&h->dx[b], cap * sizeof(float)));
+        if (!st && b < slots) st = cuda_status(cudaMalloc(&h->dy[b], cap * sizeof(float)));
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->loaded[b], cudaEventDisableTiming));
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->filtered[b], cudaEventDisableTiming));
         if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->stored[b], cudaEventDisableTiming));
     }
     if (!st) st = cuda_status(cudaMalloc(&h->dz, 4 * sizeof(float)));
+    if (!st) st = cuda_status(cudaEventCreateWithFlags(&h->start, cudaEventDisableTiming));
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking));
     if (!st) st = cuda_status(cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking));
     if (st) {
@@ -827,14 +833,11 @@ int iir_plan_execute_host(iir_plan* p, const float* x, float* y, size_t n, size_
     if (!carry) piece = n;
     piece = std::min(piece, n);
     HostStaging* h = nullptr;
-    int st = host_staging(p, piece, &h);
+    int st = host_staging(p, piece, carry ? 2 : 1, &h);
     if (st) return st;
     // Work issued to the caller's stream before this call precedes the first copy.
-    cudaEvent_t start = nullptr;
-    st = cuda_status(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
-    if (!st) st = cuda_status(cudaEventRecord(start, stream));
-    if (!st) st = cuda_status(cudaStreamWaitEvent(h->h2d, start, 0));
-    if (start) cudaEventDestroy(start);
+    st = cuda_status(cudaEventRecord(h->start, stream));
+    if (!st) st = cuda_status(cudaStreamWaitEvent(h->h2d, h->start, 0));
     size_t i = 0;
     for (size_t off = 0; off < n && !st; off += piece, ++i) {
         const int b = static_cast<int>(i & 1);
