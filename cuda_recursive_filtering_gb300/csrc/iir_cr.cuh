@@ -25,9 +25,11 @@
 // reference folds the state into the back-substitution with its h/g/p/q factors
 // (stcr_kernels.cuh:479-585).
 //
-// UNROLL selects the register form (literal indices; the reference's hand-unrolled kernels)
-// or the loop form (run-time loops over a thread-local array; the reference's *_LOOP
-// kernels). Both execute the same operations in the same order, so they are bit-identical.
+// UNROLL selects the register form (literal indices into registers; the reference's
+// hand-unrolled kernels) or the loop form (run-time loops; the reference's *_LOOP kernels),
+// which works on the row in place in the chunk's shared-memory buffer (RowInPlace), since
+// run-time indices into a thread-local array would put it in local memory. Both execute the
+// same operations in the same order, so they are bit-identical.
 #pragma once
 #include <type_traits>
 #include "iir_device.cuh"
