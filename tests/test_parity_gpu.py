@@ -301,3 +301,21 @@ def test_cascade_truncated_and_two_level_lookback(kernel, order, monkeypatch, cu
         assert e["rel_max"] <= 1e-4 and e["rel_rms"] <= RMS_TOL[order], (full, e)
         outs.append(y)
     assert np.max(np.abs(outs[0] - outs[1])) <= 1e-5 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("kernel,order", [("PH", 4), ("DTCR_UNROLL", 2), ("TC", 16), ("PLR", 4)])
+def test_gate_after_thousands_of_launches(kernel, order, cuda_device):
+    """The reference re-checks its accuracy gate after 5000 launches of one plan
+    (src/test_performance.cu:422-442): launch-versioned flags must not go stale. 5000 launches
+    on a few chunks, then the output is checked against the oracle."""
+    sos = butter(order)
+    n = 3 * 8192 + 5
+    x = np.random.default_rng(5000).uniform(-1, 1, n).astype(np.float32)
+    xd = torch.from_numpy(x).cuda()
+    y = torch.empty_like(xd)
+    plan = Plan(sos, kernel, max_n=n)
+    for _ in range(5000):
+        plan(xd, out=y)
+    plan.check()
+    e = oracle.errors(y.cpu().numpy(), golden(sos, x))
+    assert e["finite"] and e["rel_max"] <= 1e-4, e
