@@ -282,6 +282,16 @@ def run_precision(dev, log2n: int) -> dict:
     return out
 
 
+def median_p99_run(results: list[dict]) -> dict:
+    """The run with the median p99 latency (upper median for an even count), with every run's
+    GS/s, p50, p99 and maximum latency listed under "runs"."""
+    order = sorted(range(len(results)), key=lambda i: results[i]["p99_us"] or 0.0)
+    out = dict(results[order[len(results) // 2]])
+    out["runs"] = [{k: (round(r[k], 3) if r.get(k) is not None else None) for k in ("gsps", "p50_us", "p99_us", "max_us")}
+                   for r in results]
+    return out
+
+
 def run_serving(dev, seconds: float = 4.0, runs: int = 3) -> dict:
     """Continuous-batching stream server under Poisson arrivals (host chunks in, results back
     on the host): achieved GS/s and request latency percentiles. The load runs ``runs`` times;
@@ -302,9 +312,7 @@ def run_serving(dev, seconds: float = 4.0, runs: int = 3) -> dict:
         srv.samples_done = 0
         results.append(run_poisson_load(srv, streams, rate_sps=load["rate_sps"], duration_s=seconds,
                                         chunk_lo=load["chunk_lo"], chunk_hi=load["chunk_hi"], seed=load["seed"] + k))
-    order = sorted(range(runs), key=lambda i: results[i]["p99_us"] or 0.0)
-    out = dict(results[order[runs // 2]])
-    out["runs"] = [{k: round(r[k], 3) for k in ("gsps", "p50_us", "p99_us", "max_us")} for r in results]
+    out = median_p99_run(results)
     out["workload"] = ("1024 streams, order-8 butter cutoff U[0.05, 0.4] each; chunks U[256, 65536]; "
                        f"Poisson arrivals {load['rate_sps']:.0e} samples/s; {runs} runs of {seconds:g} s "
                        "(top level: the run with the median p99); host chunks in and out")
