@@ -323,9 +323,11 @@ using namespace iirhost;
 // -------------------------------------------------------------------------------------------
 // plan
 // -------------------------------------------------------------------------------------------
-// Resources of iir_plan_execute_host, created on its first call: two slots of device input and
-// output buffers (piece samples each), the carried state, a copy stream per direction and the
-// events that order the three streams.
+namespace iirhost {
+
+// Resources of iir_plan_execute_host, created on its first call: one or two slots of device input
+// and output buffers (a piece of samples each), the carried state, a copy stream per direction
+// and the events that order the three streams.
 struct HostStaging {
     size_t cap = 0;               // samples per buffer
     int slots = 0;                // 2 (pieces in flight) or 1 (the whole signal in one piece)
@@ -354,6 +356,8 @@ void host_staging_free(HostStaging* h) {
     if (h->d2h) cudaStreamDestroy(h->d2h);
     delete h;
 }
+
+}  // namespace iirhost
 
 struct iir_plan {
     int device = 0;
