@@ -22,7 +22,7 @@ from .api import Plan
 __all__ = ["tune", "tuned_plan"]
 
 _CANDIDATES_ORDER2 = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("STCR_UNROLL", 32, 32),
-                      ("DTCR_UNROLL", 32, 64), ("PH", 32, 128), ("PLR", 0, 0)]
+                      ("DTCR_UNROLL", 32, 128), ("DTCR_UNROLL", 32, 64), ("PH", 32, 128), ("PLR", 0, 0)]
 _CANDIDATES_CASCADE = [("TC", 0, 0), ("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("DTCR_UNROLL", 32, 64),
                        ("PH", 32, 128), ("STCR_UNROLL", 32, 32)]
 _memo: dict = {}
