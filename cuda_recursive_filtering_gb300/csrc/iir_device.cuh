@@ -130,12 +130,12 @@ __device__ __forceinline__ uint32_t take_ticket(IirLaunchState* st, uint32_t nch
     return c;
 }
 
-// Short back-off between polls (about `cycles` / 2 ns, doubling up to a cap). The warp
-// sleeps rather than spins, so it takes no issue slots from the warps that compute.
-// Back-off between polls of a carry slot: a doubling sleep, capped at IIR_BACKOFF_CAP / 2 ns.
-// Every poll is an L2 round trip (several hundred ns) anyway; a short cap keeps the time between
-// a predecessor's publish and its observation close to that (measured at 2^28 samples, PH 32x64
-// orders 4 / 8 / 16: 609 / 389 / 221 GS/s with a 512 ns cap, 621 / 400 / 228 with 32 ns).
+// Back-off between polls of a carry slot: a sleep of `cycles` / 2 ns, doubling up to
+// IIR_BACKOFF_CAP / 2 ns. The warp sleeps rather than spins, so it takes no issue slots from the
+// warps that compute. Every poll is an L2 round trip (several hundred ns) anyway; a short cap
+// keeps the time between a predecessor's publish and its observation close to that (measured at
+// 2^28 samples, PH 32x64 orders 4 / 8 / 16: 609 / 389 / 221 GS/s with a 512 ns cap, 621 / 400 /
+// 228 with 32 ns).
 #ifndef IIR_BACKOFF_CAP
 #define IIR_BACKOFF_CAP 64u
 #endif
