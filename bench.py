@@ -6,8 +6,13 @@ Workload (one step = one filtering pass over the whole signal): Butterworth lowp
 uniform[-1, 1) from seed 1 — the plain roofline sweep the reference benchmarks
 (GS/s, P20 of batches in src/test_performance.cu / include/measure.cuh). Headline: the DTCR
 realization at order 2 (geometry 32x64). The signal (1 GiB in + 1 GiB out) is far larger
-than L2, so no flush is needed between steps. Extra rows time every realization at orders
-2/4/8/16 on the same signal.
+than L2, so no flush is needed between steps.
+
+Every row of the sweep (realization x order x geometry, at 2^28 and 2^25 samples; order 2 at
+2^16) carries {gsps, frac, rel_max, rel_rms}: frac against the measured HBM roof (8 bytes per
+sample), and the error of ALL of that row's outputs against the FP64 oracle (the reference's
+golden path, tools/ref_generate.py:89), compared on the device. The precision form is
+measured at orders 8..16 on its own workload with the same full-length error.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--no-sweep]
 
@@ -17,6 +22,7 @@ workload on its own GPU (the path has no exchange step between GPUs: replicas on
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -37,6 +43,9 @@ _GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
 SWEEP_GEOM = {"PH": _GEOMS, "STCR": _GEOMS, "STCR_UNROLL": _GEOMS, "DTCR": _GEOMS, "DTCR_UNROLL": _GEOMS,
               "PLR": [(0, 0)]}
 BYTES_PER_SAMPLE = 8  # 4 read + 4 written (algorithmic)
+L2_BYTES = 129 * 1024 * 1024
+GATE = 1e-4           # the reference's accuracy gate, max|err| <= 1e-4 max|ref| (src/test_accuracy.cu:178-188)
+CPU_PIECE = 1 << 21   # samples per piece of the CPU baselines (one piece per host thread)
 
 
 def peaks() -> dict:
@@ -48,16 +57,21 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def ncu_traffic_per_launch() -> float | None:
-    """DRAM bytes (read + write) per launch of the headline kernel from the committed ncu
-    summary, scaled to 2^28 samples (the summary records bytes per sample)."""
-    path = os.path.join(ROOT, "profiles", "dtcr_unroll_order2_full.md")
+def ncu_traffic_per_launch() -> dict | None:
+    """DRAM bytes (read + write) of one launch of the headline kernel at 2^28 samples, from the
+    committed one-pass ncu capture of that launch (profiles/dtcr_unroll_order2_traffic_2p28.md)."""
+    path = os.path.join(ROOT, "profiles", "dtcr_unroll_order2_traffic_2p28.md")
     if not os.path.exists(path):
         return None
+    vals = {}
     for line in open(path):
-        if line.startswith("dram_bytes_per_sample:"):
-            return float(line.split(":")[1]) * (1 << LOG2N)
-    return None
+        if ":" in line and line.split(":")[0].strip() in ("dram_bytes_read", "dram_bytes_write", "samples"):
+            k, v = line.split(":", 1)
+            vals[k.strip()] = float(v.split()[0])
+    if "dram_bytes_read" not in vals or "dram_bytes_write" not in vals:
+        return None
+    return {"bytes": vals["dram_bytes_read"] + vals["dram_bytes_write"], "read": vals["dram_bytes_read"],
+            "write": vals["dram_bytes_write"], "samples": vals.get("samples")}
 
 
 class ClockSampler:
@@ -130,6 +144,31 @@ def time_plan(plan, x, y, steps: int, warmup: int, stream):
     return s.elapsed_time(e) / steps
 
 
+def time_rotating(plan, xs, ys, batches: int, per_batch: int, stream) -> list[float]:
+    """The reference's timing method (include/measure.cuh:37-110): launches cycle through
+    several identical input / output buffers whose total exceeds L2; `batches` batches of
+    `per_batch` launches, each timed with CUDA events. Returns ms per launch of each batch."""
+    import torch
+    nb = len(xs)
+    for i in range(min(3 * nb, 600)):
+        plan(xs[i % nb], ys[i % nb], stream=stream)
+    plan.check(stream)
+    out = []
+    k = 0
+    for _ in range(batches):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(per_batch):
+            plan(xs[k % nb], ys[k % nb], stream=stream)
+            k += 1
+        e.record(stream)
+        e.synchronize()
+        out.append(s.elapsed_time(e) / per_batch)
+    plan.check(stream)
+    return out
+
+
 def host_threads() -> int:
     try:
         return max(1, len(os.sched_getaffinity(0)))
@@ -137,79 +176,188 @@ def host_threads() -> int:
         return max(1, os.cpu_count() or 1)
 
 
-def cpu_filter_pass(sos, pieces, threads: int) -> float:
-    """One pass of the FP64 cascade (the oracle's C port of sosfilt) over every piece, the pieces
-    spread over `threads` host threads (ctypes releases the GIL during each call). Each piece
-    is an independent signal from zero state: the recurrence within a piece is serial, so the
-    host's cores are used across pieces. Returns the wall time in seconds."""
-    import concurrent.futures as cf
+# ------------------------------------------------------------------------------------------
+# FP64 oracle outputs, computed on the host in background threads (the C oracle releases the
+# GIL) and compared with the device output on the device
+# ------------------------------------------------------------------------------------------
+class Golden:
+    """FP64 oracle output of a workload, prefetched a few jobs ahead on host threads."""
 
-    import oracle
+    def __init__(self, jobs, ahead: int = 3):
+        self.jobs = list(jobs)          # (key, sos, x_host_f32)
+        self.ahead = ahead
+        self.pool = cf.ThreadPoolExecutor(ahead)
+        self.fut = {}
+        self.next = 0
+        self._fill()
+
+    def _fill(self):
+        while self.next < len(self.jobs) and len(self.fut) < self.ahead:
+            key, sos, xh = self.jobs[self.next]
+            self.fut[key] = self.pool.submit(self._run, sos, xh)
+            self.next += 1
+
+    @staticmethod
+    def _run(sos, xh):
+        import oracle
+        return oracle.reference_golden(sos, xh)[1]
+
+    def get(self, key):
+        ref = self.fut.pop(key).result()
+        self._fill()
+        return ref
+
+    def close(self):
+        self.pool.shutdown(wait=False, cancel_futures=True)
+
+
+class DeviceRef:
+    """An FP64 oracle output on the device with its scale (max|ref|, RMS(ref))."""
+
+    def __init__(self, ref_host, dev):
+        import torch
+        self.ref = torch.from_numpy(ref_host).to(dev)
+        self.maxabs = float(self.ref.abs().max())
+        self.rms = float(self.ref.square().mean().sqrt())
+
+    def errors(self, y, n: int | None = None) -> dict:
+        """max|y - ref| over the first n outputs, relative to max|ref| (the reference's gate) and
+        to RMS(ref); non-finite output gives inf."""
+        import torch
+        n = y.numel() if n is None else n
+        err = 0.0
+        step = 1 << 26
+        for i in range(0, n, step):
+            d = (y[i:min(n, i + step)].double() - self.ref[i:min(n, i + step)]).abs().max()
+            err = max(err, float(d))
+        if not (err == err) or err == float("inf") or not bool(torch.isfinite(y[:n]).all()):
+            return {"rel_max": float("inf"), "rel_rms": float("inf")}
+        if n == self.ref.numel():
+            mref, rms = self.maxabs, self.rms
+        else:
+            r = self.ref[:n]
+            mref, rms = float(r.abs().max()), float(r.square().mean().sqrt())
+        return {"rel_max": err / max(mref, 1e-300), "rel_rms": err / max(rms, 1e-300)}
+
+
+def row_entry(gsps: float, hbm_gbs: float, e: dict) -> dict:
+    return {"gsps": round(gsps, 1), "frac": round(gsps * BYTES_PER_SAMPLE / hbm_gbs, 4),
+            "rel_max": float(f"{e['rel_max']:.3g}"), "rel_rms": float(f"{e['rel_rms']:.3g}"),
+            "gate": "pass" if e["rel_max"] <= GATE else "fail"}
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baselines (the reference's CPU golden path and the float32 sequential cascade)
+# ------------------------------------------------------------------------------------------
+def cpu_pieces(x_host, threads: int):
+    """One piece of CPU_PIECE samples per host thread, cut from the start of the workload's
+    signal; each piece is filtered as an independent signal from zero state (the recurrence
+    within a signal is serial, so the host's cores are used across pieces)."""
+    import numpy as np
+    n = min(x_host.size, CPU_PIECE * threads)
+    return [np.ascontiguousarray(p) for p in np.array_split(x_host[:n], threads)]
+
+
+def cpu_pass(fn, pieces, threads: int) -> float:
+    """Wall time of one pass of fn over every piece, the pieces spread over `threads` threads
+    (fn must release the GIL: the C oracle through ctypes, scipy's sosfilt)."""
     t0 = time.perf_counter()
     if threads == 1:
-        for xs in pieces:
-            oracle.sosfilt_f64(sos, xs)
+        for p in pieces:
+            fn(p)
     else:
         with cf.ThreadPoolExecutor(threads) as ex:
-            list(ex.map(lambda xs: oracle.sosfilt_f64(sos, xs), pieces))
+            list(ex.map(fn, pieces))
     return time.perf_counter() - t0
 
 
-def cpu_baseline_sample(sos, x_cpu, budget_s: float = 10.0) -> dict:
-    """The reference's CPU golden path (FP64 cascade, tools/ref_generate.py:89 via scipy's
-    sosfilt; restated in C under oracle/) on a bounded sample of the workload: the first 2^24
-    samples cut into one piece per host thread, filtered repeatedly for about `budget_s`."""
+def cpu_kernels(sos):
+    """The CPU implementations timed: the oracle's C port of the FP64 golden path, scipy's own
+    sosfilt (the call tools/ref_generate.py:89 makes) and the float32 sequential cascade."""
+    import numpy as np
+    from scipy import signal
+
+    import oracle
+    oracle.build()
+    norm, g = oracle.normalise_sos(sos)
+    sos_f32 = norm.astype(np.float32)
+    s64 = np.asarray(sos, np.float64)
+    return {
+        "port": lambda p: oracle.sosfilt_f64(s64, p),
+        "scipy_sosfilt": lambda p: signal.sosfilt(s64, p),
+        "float32_cascade": lambda p: oracle.cascade_f32(p.astype(np.float32) * np.float32(g), sos_f32),
+    }
+
+
+def cpu_baseline_sample(sos, x_host, budget_s: float = 10.0) -> dict:
+    """The reference's CPU path on a bounded sample of the workload, on all host threads:
+    one 2^21-sample piece per thread (each an independent zero-state signal), passes repeated
+    for about `budget_s` seconds per implementation. Same pieces and piece size as the
+    reference arm (--impl reference)."""
     import numpy as np
     threads = host_threads()
-    xs = np.ascontiguousarray(x_cpu[: 1 << 24], dtype=np.float64)
-    pieces = np.array_split(xs, threads)
-    done, spent = 0, 0.0
-    while True:
-        spent += cpu_filter_pass(sos, pieces, threads)
-        done += xs.size
-        if spent >= budget_s or done >= (1 << 28):
-            break
-    return {"value": done / spent / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{done} samples: the first 2^24 samples of the workload in {threads} pieces (one per "
-                      f"host thread, each an independent zero-state signal), FP64 cascade, {spent:.1f} s"}
+    xs = np.ascontiguousarray(x_host[:CPU_PIECE * threads], dtype=np.float64)
+    pieces = cpu_pieces(xs, threads)
+    sample = sum(p.size for p in pieces)
+    fns = cpu_kernels(sos)
+    rates = {}
+    for name, fn in fns.items():
+        done, spent = 0, 0.0
+        cpu_pass(fn, pieces[:1], 1)  # warm-up
+        while spent < budget_s / len(fns):
+            spent += cpu_pass(fn, pieces, threads)
+            done += sample
+        rates[name] = {"gsps": round(done / spent / 1e9, 4), "seconds": round(spent, 2)}
+    one = cpu_pass(fns["scipy_sosfilt"], pieces[:1], 1)
+    return {"value": rates["port"]["gsps"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample} samples per pass: the first {sample} samples of the workload in {threads} pieces "
+                      f"of {CPU_PIECE} (one per host thread, each an independent zero-state signal); value = the "
+                      f"oracle's C port of the FP64 golden cascade",
+            "implementations": rates,
+            "scipy_sosfilt_1_thread_gsps": round(pieces[0].size / one / 1e9, 4)}
 
 
 def run_reference(args, rank: int, world: int) -> None:
     """Reference arm: the reference's own CPU implementation of the path (its golden
-    generator's FP64 sosfilt cascade, restated in C under oracle/) on all host threads."""
+    generator's FP64 sosfilt cascade, restated in C under oracle/) on all host threads, on the
+    same pieces as the in-line CPU baseline; scipy's sosfilt itself is timed beside it."""
     if rank != 0:
         return
     import numpy as np
-    import oracle
     from scipy import signal
-    oracle.build()
     sos = signal.butter(HEADLINE["order"], 0.1, output="sos")
     threads = host_threads()
-    per_thread = 1 << 21
-    sample = per_thread * threads  # per step: a bounded sample of the 2^28-sample workload
-    x = np.random.default_rng(1).uniform(-1, 1, sample).astype(np.float64)
-    pieces = np.array_split(x, threads)
+    sample = CPU_PIECE * threads
+    x = np.random.default_rng(1).uniform(-1, 1, sample).astype(np.float32).astype(np.float64)
+    pieces = cpu_pieces(x, threads)
+    fns = cpu_kernels(sos)
     for _ in range(args.warmup):
-        cpu_filter_pass(sos, pieces, threads)
-    spent = sum(cpu_filter_pass(sos, pieces, threads) for _ in range(args.steps))
+        cpu_pass(fns["port"], pieces, threads)
+    spent = sum(cpu_pass(fns["port"], pieces, threads) for _ in range(args.steps))
     dt = spent / args.steps
     value = sample / dt / 1e9
+    sp = min(cpu_pass(fns["scipy_sosfilt"], pieces, threads) for _ in range(3))
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"butter order {HEADLINE['order']} cutoff 0.1, uniform[-1,1) seed 1; "
                                f"step = {sample} samples of the 2^{LOG2N}-sample workload in {threads} pieces "
-                               f"of 2^21 (one per host thread, each from zero state)",
+                               f"of {CPU_PIECE} (one per host thread, each an independent zero-state signal)",
                    "n_samples_per_step": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{sample} samples per step in {threads} independent pieces, FP64 cascade "
-                                   f"(serial recurrence per piece, one piece per host thread)"},
+                         "sample": f"{sample} samples per step in {threads} independent pieces of {CPU_PIECE}, "
+                                   "FP64 cascade (the oracle's C port of scipy's sosfilt as "
+                                   "tools/ref_generate.py:89 calls it)",
+                         "scipy_sosfilt_gsps": round(sample / sp / 1e9, 4)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------------------------------------------
+# forms (batching, serving, precision)
+# ------------------------------------------------------------------------------------------
 def run_batching(dev) -> dict:
     """Many channels of uneven length, each with its own filter, in one launch (Batch.packed);
     device-resident, CUDA events over 10 launches; a few channels checked against the oracle."""
@@ -247,37 +395,45 @@ def run_batching(dev) -> dict:
             "samples": int(off[-1]), "check_rel_max_8_channels": worst}
 
 
-def run_precision(dev, log2n: int) -> dict:
+def run_precision(dev, log2n: int, hbm_gbs: float) -> dict:
     """Precision form (kernel TC: the chunk solve as tcgen05 TF32 GEMMs with split products)
     against the plain PH and STCR_UNROLL realizations on the precision workload: butter(order,
-    0.05) on N(0,1) noise plus 8 tones spanning 60 dB (seed 2), device-resident, CUDA events
-    over 5 launches each; max|err| / RMS(ref) against the FP64 oracle on the first 2^20 outputs."""
+    0.05) on N(0,1) noise plus 8 tones spanning 60 dB (seed 2), orders 8..16, device-resident,
+    CUDA events over 5 launches each; max|err| / RMS(ref) over ALL outputs against the FP64
+    oracle. `tc_vs_plain_at_1e-5` compares TC with the fastest plain row whose error is within
+    the 1e-5 RMS-relative bar."""
     import torch
 
-    import oracle
     from cuda_recursive_filtering_gb300 import Plan, workloads
 
     n = 1 << log2n
     x = workloads.noise_plus_tones(n, 2, device=dev)
     y = torch.empty_like(x)
-    head = x[: 1 << 20].cpu().numpy()
+    xh = x.cpu().numpy()
     stream = torch.cuda.current_stream()
+    orders = (8, 10, 12, 14, 16)
+    gold = Golden([(o, workloads.butter_sos(o, 0.05), xh) for o in orders], ahead=3)
     out = {"workload": f"butter(order, 0.05) SOS on 2^{log2n} samples of N(0,1) noise + 8 tones (60 dB span), "
-                       "seed 2; error = max|err| / RMS(ref) over the first 2^20 outputs"}
-    for order in (8, 16):
-        sos = workloads.butter_sos(order, 0.05)
-        _, ref = oracle.reference_golden(sos, head)
-        row = {}
-        for kname, b, nb in (("TC", 0, 0), ("PH", 32, 64), ("STCR_UNROLL", 32, 64)):
-            pl = Plan(sos, kname, b, nb, max_n=n, device=dev)
-            t = time_plan(pl, x, y, 5, 2, stream)
-            pl.check()
-            e = oracle.errors(y[: 1 << 20].cpu().numpy(), ref)
-            pl.close()
-            row[kname] = {"gsps": round(n / (t * 1e-3) / 1e9, 1), "err": float(f"{e['rel_rms']:.3g}")}
-        row["tc_vs_ph"] = round(row["TC"]["gsps"] / row["PH"]["gsps"], 2)
-        row["tc_vs_stcr_unroll"] = round(row["TC"]["gsps"] / row["STCR_UNROLL"]["gsps"], 2)
-        out[f"order{order}"] = row
+                       "seed 2; error = max|err| / RMS(ref) over all outputs"}
+    try:
+        for order in orders:
+            sos = workloads.butter_sos(order, 0.05)
+            ref = DeviceRef(gold.get(order), dev)
+            row = {}
+            for kname, b, nb in (("TC", 0, 0), ("PH", 32, 64), ("STCR_UNROLL", 32, 64)):
+                pl = Plan(sos, kname, b, nb, max_n=n, device=dev)
+                t = time_plan(pl, x, y, 5, 2, stream)
+                pl.check()
+                pl.close()
+                row[kname] = row_entry(n / (t * 1e-3) / 1e9, hbm_gbs, ref.errors(y))
+            plain = [row[k]["gsps"] for k in ("PH", "STCR_UNROLL") if row[k]["rel_rms"] <= 1e-5]
+            row["tc_vs_ph"] = round(row["TC"]["gsps"] / row["PH"]["gsps"], 2)
+            row["tc_vs_plain_at_1e-5"] = (round(row["TC"]["gsps"] / max(plain), 2)
+                                          if plain and row["TC"]["rel_rms"] <= 1e-5 else None)
+            out[f"order{order}"] = row
+            del ref
+    finally:
+        gold.close()
     del x, y
     return out
 
@@ -319,13 +475,107 @@ def run_serving(dev, seconds: float = 4.0, runs: int = 3) -> dict:
     return out
 
 
-def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+# ------------------------------------------------------------------------------------------
+# the sweep: realization x order x geometry
+# ------------------------------------------------------------------------------------------
+def sweep_keys(order: int):
+    for kname, geoms in SWEEP_GEOM.items():
+        if kname == "PLR" and order > 8:
+            continue  # float32 direct form: non-finite at order 16 (plr_emulator.py:228-248)
+        for b, nb in geoms:
+            yield kname, b, nb, f"order{order}_{kname}" + (f"_{b}x{nb}" if b else "")
+
+
+def run_sweep(dev, x, xh, steps: int, hbm_gbs: float) -> dict:
+    """Every realization x order x geometry at 2^LOG2N samples (and, with rotating buffers past
+    L2, at 2^25), each with the error of all its outputs against the FP64 oracle."""
+    import torch
+    from scipy import signal
+
+    from cuda_recursive_filtering_gb300 import Plan
+
+    n = x.numel()
+    stream = torch.cuda.current_stream()
+    y = torch.empty_like(x)
+    n25 = min(n, 1 << 25)
+    nbuf = max(4, -(-2 * L2_BYTES // (4 * n25)))
+    xs25 = [x[:n25].clone() for _ in range(nbuf)]
+    ys25 = [torch.empty(n25, device=dev) for _ in range(nbuf)]
+    orders = (2, 4, 8, 16)
+    gold = Golden([(o, signal.butter(o, 0.1, output="sos"), xh) for o in orders], ahead=3)
+    rows_full, rows_25 = {}, {}
+    try:
+        for order in orders:
+            s_o = signal.butter(order, 0.1, output="sos")
+            ref = DeviceRef(gold.get(order), dev)
+            for kname, b, nb, key in sweep_keys(order):
+                try:
+                    pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
+                    t = time_plan(pl, x, y, max(3, steps // 2), 2, stream)
+                    rows_full[key] = row_entry(n / (t * 1e-3) / 1e9, hbm_gbs, ref.errors(y))
+                    if n25 < n:
+                        ms = time_rotating(pl, xs25, ys25, 5, 2 * nbuf, stream)
+                        rows_25[key] = row_entry(n25 / (statistics.median(ms) * 1e-3) / 1e9, hbm_gbs,
+                                                 ref.errors(ys25[0], n25))
+                    pl.close()
+                except Exception as exc:  # report, do not hide
+                    rows_full[key] = f"error: {exc}"
+            del ref
+    finally:
+        gold.close()
+    del xs25, ys25, y
+    out = {f"2^{n.bit_length() - 1}": rows_full}
+    if rows_25:
+        out["2^25"] = rows_25
+        out["2^25_method"] = (f"{nbuf} identical input and output buffers (> 2x L2) cycled, 5 batches of "
+                              f"{2 * nbuf} launches, median batch")
+    return out
+
+
+def run_small(dev, hbm_gbs: float) -> dict:
+    """The latency regime (2^16 samples, butter(2, 0.1), uniform[-1,1) seed 0): the reference's
+    timing method — 1032 identical buffers (2 x L2) cycled, 20 batches of 200 launches, the
+    20th-percentile and median batch (include/measure.cuh:70-109) — with the error of the
+    output against the FP64 oracle (gate max|err| / RMS <= 1e-5)."""
     import numpy as np
     import torch
     from scipy import signal
 
+    import oracle
+    from cuda_recursive_filtering_gb300 import Plan, workloads
+
+    n = 1 << 16
+    sos = signal.butter(2, 0.1, output="sos")
+    x = workloads.uniform_signal(n, 0, device=dev)
+    _, ref = oracle.reference_golden(sos, x.cpu().numpy())
+    nbuf = -(-2 * L2_BYTES // (4 * n))
+    xs = [x.clone() for _ in range(nbuf)]
+    ys = [torch.empty(n, device=dev) for _ in range(nbuf)]
+    stream = torch.cuda.current_stream()
+    rows = {}
+    for kname, b, nb in (("PH", 32, 64), ("DTCR", 32, 64), ("DTCR_UNROLL", 32, 64), ("STCR", 32, 64),
+                         ("STCR_UNROLL", 32, 64), ("PLR", 0, 0), ("TC", 0, 0)):
+        pl = Plan(sos, kname, b, nb, max_n=n, device=dev)
+        ms = time_rotating(pl, xs, ys, 20, 200, stream)
+        e = oracle.errors(ys[0].cpu().numpy(), ref)
+        pl.close()
+        ms_sorted = sorted(ms)
+        p20 = ms_sorted[len(ms_sorted) // 5]
+        key = f"order2_{kname}" + (f"_{b}x{nb}" if b else "")
+        rows[key] = dict(row_entry(n / (p20 * 1e-3) / 1e9, hbm_gbs, e),
+                         gsps_median=round(n / (statistics.median(ms) * 1e-3) / 1e9, 1),
+                         us_per_launch_p20=round(p20 * 1e3, 2))
+    del xs, ys
+    return {"rows": rows, "method": f"{nbuf} identical input and output buffers cycled, 20 batches of 200 launches; "
+                                    "gsps = 20th-percentile batch, gsps_median = median batch"}
+
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+    import torch
+    from scipy import signal
+
     import cuda_recursive_filtering_gb300 as pkg
-    from cuda_recursive_filtering_gb300 import Plan, sosfilt, workloads
+    from cuda_recursive_filtering_gb300 import Plan, workloads
 
     torch.cuda.set_device(local_rank)
     pkg.load_library()
@@ -333,22 +583,17 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     n = 1 << LOG2N
     stream = torch.cuda.current_stream()
     x = workloads.uniform_signal(n, 1, device=dev)
+    xh = x.cpu().numpy()
     y = torch.empty_like(x)
     pk = peaks()
 
     # ---- headline: device-resident throughput ----
     sos = signal.butter(HEADLINE["order"], 0.1, output="sos")
+    gold = Golden([("headline", sos, xh)], ahead=1)
     plan = Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=n, device=dev)
     for _ in range(2):
         plan(x, y)
     torch.cuda.synchronize()
-    # correctness of this exact run on a prefix (causal filter: first M outputs depend on the
-    # first M inputs only)
-    import oracle
-    m = 1 << 20
-    xp = x[:m].cpu().numpy()
-    _, ref = oracle.reference_golden(sos, xp)
-    chk = oracle.errors(y[:m].cpu().numpy(), ref)
 
     clocks = ClockSampler(local_rank)
     clocks.start()
@@ -367,57 +612,53 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         ms = float(t.item())
     value = world * n / (ms * 1e-3) / 1e9
     achieved = BYTES_PER_SAMPLE * n / (ms * 1e-3) / 1e9
+    # correctness of this exact run: every output of the last timed launch against the oracle
+    head_ref = DeviceRef(gold.get("headline"), dev)
+    gold.close()
+    chk = head_ref.errors(y)
+    del head_ref
 
     # ---- end to end: host buffers through the public API (C ABI), copies inside ----
     # iir_plan_execute_host: pinned host input and output; the copies of the signal's pieces
     # overlap the filtering on three streams, each piece starting from the previous one's state.
     e2e = None
     if rank == 0 or world > 1:
-        xh = torch.empty(n, dtype=torch.float32, pin_memory=True)
-        xh.copy_(x.cpu())
+        xhp = torch.empty(n, dtype=torch.float32, pin_memory=True)
+        xhp.copy_(torch.from_numpy(xh))
         yh = torch.empty(n, dtype=torch.float32, pin_memory=True)
         hplan = Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=n)
         e2e_steps = max(2, min(args.steps, 5))
         for _ in range(2):
-            hplan.filter_host(xh, out=yh)
+            hplan.filter_host(xhp, out=yh)
         hplan.check()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            hplan.filter_host(xh, out=yh)
+            hplan.filter_host(xhp, out=yh)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / e2e_steps
         hplan.check()
         e2e = {"value": world * n / dt / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step": 4 * n,
-               "ms_per_step": dt * 1e3, "api": "iir_plan_execute_host, pieces of 2^24 samples"}
-        if rank == 0:
-            yref = torch.empty(1 << 20, device=dev)
-            Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=1 << 20)(
-                x[:1 << 20], out=yref)
-            e2e["check_prefix_max_abs_diff"] = float((yh[:1 << 20].to(dev) - yref).abs().max())
+               "ms_per_step": dt * 1e3, "api": "iir_plan_execute_host, pieces of 2^24 samples",
+               "check_max_abs_diff_vs_device_output": float((yh.to(dev) - y).abs().max())}
         hplan.close()
-        del xh, yh
+        del xhp, yh
 
-    # ---- per-order / per-realization rows ----
-    rows = {}
+    # ---- sweep rows with full-length errors, the latency regime, the forms ----
+    sweep = {}
     if not args.no_sweep:
-        for order in (2, 4, 8, 16):
-            s_o = signal.butter(order, 0.1, output="sos")
-            for kname, geoms in SWEEP_GEOM.items():
-                if kname == "PLR" and order > 8:
-                    continue  # float32 direct form fails the accuracy gate at order 16
-                for b, nb in geoms:
-                    key = f"order{order}_{kname}" + (f"_{b}x{nb}" if b else "")
-                    try:
-                        pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
-                        t = time_plan(pl, x, y, max(3, args.steps // 2), 2, stream)
-                        pl.close()
-                        rows[key] = round(n / (t * 1e-3) / 1e9, 1)
-                    except Exception as exc:  # report, do not hide
-                        rows[key] = f"error: {exc}"
+        try:
+            sweep = run_sweep(dev, x, xh, args.steps, pk["hbm_gbs"])
+        except Exception as exc:  # report, do not hide
+            sweep = {"error": str(exc)}
+        try:
+            sweep["2^16"] = run_small(dev, pk["hbm_gbs"])
+        except Exception as exc:
+            sweep["2^16"] = {"error": str(exc)}
+    del y
     forms = {}
     if not args.no_forms:
         try:
-            forms["precision"] = run_precision(dev, LOG2N)
+            forms["precision"] = run_precision(dev, LOG2N, pk["hbm_gbs"])
         except Exception as exc:  # report, do not hide
             forms["precision"] = {"error": str(exc)}
         try:
@@ -430,8 +671,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             forms["serving"] = {"error": str(exc)}
     if rank != 0:
         return
-    cpu = cpu_baseline_sample(sos, x[: 1 << 24].cpu().numpy(), budget_s=args.cpu_seconds)
+    cpu = cpu_baseline_sample(sos, xh, budget_s=args.cpu_seconds)
     traffic = ncu_traffic_per_launch()
+    tr = None
+    if traffic is not None:
+        tr = traffic["bytes"] * (n / traffic["samples"] if traffic.get("samples") else 1.0)
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -443,14 +687,17 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                    "l2": "inputs (1 GiB) larger than L2 (129 MB): no flush between steps",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+                     "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": tr,
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 2^28 "
+                                        "(profiles/dtcr_unroll_order2_traffic_2p28.md)") if tr else None,
                      "peak_source": pk["source"] + " (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": args.steps * plan.launches_per_execute(),
         "clocks": clk,
-        "check": {"rel_max": chk["rel_max"], "rel_rms": chk["rel_rms"], "prefix_samples": m},
-        "per_order_gsps": rows,
+        "check": {"rel_max": float(f"{chk['rel_max']:.3g}"), "rel_rms": float(f"{chk['rel_rms']:.3g}"),
+                  "samples": n, "what": "all outputs of the last timed launch against the FP64 oracle"},
+        "sweep": sweep,
     }
     out.update(forms)
     print(json.dumps(out), flush=True)
@@ -464,7 +711,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the precision, batching and serving legs")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
     args = ap.parse_args()

@@ -75,6 +75,7 @@ def load(path: str | None = None):
         "iir_status_string": ([i], ctypes.c_char_p),
         "iir_version": ([], i),
         "iir_cache_clear": ([], i),
+        "iir_sos_filter_debug_withhold": ([ll, ll], i),
         "iir_batch_create": ([pp, fp, ip, i, sz, sz], i),
         "iir_batch_execute": ([vp, ctypes.POINTER(IirSegment), i, vp], i),
         "iir_batch_check": ([vp, vp], i),

@@ -478,7 +478,7 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
     }
     if (++b->launches >= (1ull << 30)) {
         int st = cuda_status(cudaMemsetAsync(b->d_carry, 0, b->carry_bytes, stream));
-        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, sizeof(IirLaunchState), stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, IIR_STATE_RESET_BYTES, stream));
         if (st) return st;
         b->launches = 1;
     }
@@ -607,7 +607,7 @@ int iir_batch_launch_bound(iir_batch_bound* h, void* stream_) {
     cudaStream_t stream = static_cast<cudaStream_t>(stream_);
     if (++b->launches >= (1ull << 30)) {
         int st = cuda_status(cudaMemsetAsync(b->d_carry, 0, b->carry_bytes, stream));
-        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, sizeof(IirLaunchState), stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(b->d_state, 0, IIR_STATE_RESET_BYTES, stream));
         if (st) return st;
         b->launches = 1;
     }

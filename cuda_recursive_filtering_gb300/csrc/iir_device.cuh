@@ -115,8 +115,20 @@ __device__ __forceinline__ bool launch_failed(const IirLaunchState* st, uint32_t
     const unsigned long long e = ld_relaxed_u64(&st->error);
     return e != 0ull && static_cast<uint32_t>(e >> 32) == epoch;
 }
+// Records a failure of launch `epoch`. The first failure of a launch is kept (it is the cause:
+// a withheld carry times out its successors' lookbacks first, and their blocks' later waits
+// give up after it); the word also goes to the host-mapped copy, if the plan has one.
 __device__ __forceinline__ void raise_error(IirLaunchState* st, uint32_t epoch, uint32_t code) {
-    atomicExch(&st->error, (static_cast<unsigned long long>(epoch) << 32) | code);
+    const unsigned long long w = (static_cast<unsigned long long>(epoch) << 32) | code;
+    unsigned long long cur = ld_relaxed_u64(&st->error);
+    while (true) {
+        if (cur != 0ull && static_cast<uint32_t>(cur >> 32) == epoch) return;  // already recorded
+        const unsigned long long prev = atomicCAS(&st->error, cur, w);
+        if (prev == cur) break;
+        cur = prev;
+    }
+    unsigned long long* h = *reinterpret_cast<unsigned long long* volatile*>(&st->host_error);
+    if (h) *reinterpret_cast<volatile unsigned long long*>(h) = w;  // seen by the host without a sync
 }
 
 // Takes the block's ticket: one atomic returns the launch epoch (high word) and the chunk

@@ -316,6 +316,12 @@ int cuda_status(cudaError_t e) {
     return e == cudaErrorMemoryAllocation ? IIR_ERR_OUT_OF_MEMORY : IIR_ERR_CUDA;
 }
 
+int device_error_status(unsigned long long word) {
+    if (word == 0ull) return IIR_OK;
+    const unsigned code = static_cast<unsigned>(word & 0xffffffffull);
+    return code == IIR_DEV_ERR_TIMEOUT ? IIR_ERR_LOOKBACK_TIMEOUT : IIR_ERR_CUDA;
+}
+
 }  // namespace iirhost
 
 using namespace iirhost;
@@ -381,6 +387,7 @@ struct iir_plan {
     unsigned long long launches = 0;  // since the carry slots were last zeroed
     size_t carry_bytes = 0;
     HostStaging* host = nullptr;      // iir_plan_execute_host: device buffers, streams, events
+    unsigned long long* h_err = nullptr;  // host-mapped copy of the device error word (IirLaunchState::host_error)
 };
 
 namespace {
@@ -438,6 +445,34 @@ int alloc_carry(iir_plan* p, size_t cap_chunks, cudaStream_t stream) {
     return IIR_OK;
 }
 
+// A host-mapped word that the plan's failing launches also write their error to
+// (IirLaunchState::host_error), so a later call can see the failure without synchronising.
+int attach_host_error(iir_plan* p) {
+    void* h = nullptr;
+    int st = cuda_status(cudaHostAlloc(&h, sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable));
+    if (st) return st;
+    p->h_err = static_cast<unsigned long long*>(h);
+    *p->h_err = 0ull;
+    void* d = nullptr;
+    st = cuda_status(cudaHostGetDevicePointer(&d, h, 0));
+    if (!st)
+        st = cuda_status(cudaMemcpy(reinterpret_cast<char*>(p->d_state) + offsetof(IirLaunchState, host_error), &d,
+                                    sizeof(d), cudaMemcpyHostToDevice));
+    return st;
+}
+
+// The device error a launch of the plan left in its host-mapped word (IIR_OK if none), cleared.
+// The word is written by the device asynchronously: an error shows up here once the failing
+// launch has recorded it, with no synchronisation.
+int take_host_error(iir_plan* p) {
+    if (!p->h_err) return IIR_OK;
+    volatile unsigned long long* w = p->h_err;
+    const unsigned long long v = *w;
+    if (v == 0ull) return IIR_OK;
+    *w = 0ull;
+    return device_error_status(v);
+}
+
 int plan_common_alloc(iir_plan* p, size_t max_n) {
     int st = cuda_status(cudaGetDevice(&p->device));
     if (st) return st;
@@ -449,6 +484,8 @@ int plan_common_alloc(iir_plan* p, size_t max_n) {
     st = cuda_status(cudaMalloc(&p->d_state, sizeof(IirLaunchState)));
     if (st) return st;
     st = cuda_status(cudaMemset(p->d_state, 0, sizeof(IirLaunchState)));
+    if (st) return st;
+    st = attach_host_error(p);
     if (st) return st;
     const size_t chunk = chunk_samples(p);
     return alloc_carry(p, (std::max<size_t>(max_n, 1) + chunk - 1) / chunk, nullptr);
@@ -465,6 +502,7 @@ void plan_free(iir_plan* p) {
         host_staging_free(p->host);
     }
     if (p->d_state) cudaFree(p->d_state);
+    if (p->h_err) cudaFreeHost(p->h_err);
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_fac) cudaFree(p->d_fac);
@@ -646,6 +684,11 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
         }
         p->d_state = tc_plan_state(p->tc);
         p->grid_max = tc_plan_grid(p->tc);
+        st = attach_host_error(p);
+        if (st) {
+            plan_free(p);
+            return st;
+        }
         *out = p;
         return IIR_OK;
     }
@@ -720,7 +763,7 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
     // long before the epoch could wrap (the reference zeroes its status buffer once).
     if (++p->launches >= (1ull << 30)) {
         int st = cuda_status(cudaMemsetAsync(p->d_carry, 0, p->carry_bytes, stream));
-        if (!st) st = cuda_status(cudaMemsetAsync(p->d_state, 0, sizeof(IirLaunchState), stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(p->d_state, 0, IIR_STATE_RESET_BYTES, stream));
         if (st) return st;
         p->launches = 1;
     }
@@ -881,12 +924,12 @@ int iir_plan_check(iir_plan* p, void* stream_) {
     IirLaunchState hs;
     st = cuda_status(cudaMemcpy(&hs, p->d_state, sizeof(hs), cudaMemcpyDeviceToHost));
     if (st) return st;
+    take_host_error(p);  // the same failure, already read from the device word
     if (hs.error == 0ull) return IIR_OK;
     const unsigned long long zero = 0ull;
     cudaMemcpy(reinterpret_cast<char*>(p->d_state) + offsetof(IirLaunchState, error), &zero, sizeof(zero),
                cudaMemcpyHostToDevice);
-    const unsigned code = static_cast<unsigned>(hs.error & 0xffffffffull);
-    return code == IIR_DEV_ERR_TIMEOUT ? IIR_ERR_LOOKBACK_TIMEOUT : IIR_ERR_CUDA;
+    return device_error_status(hs.error);
 }
 
 int iir_plan_set_timeout_ns(iir_plan* p, long long timeout_ns) {
@@ -944,13 +987,36 @@ struct CacheKey {
                std::tie(o.device, o.stream, o.kernel, o.B, o.N, o.n_sections, o.sos);
     }
 };
+struct CacheEntry {
+    iir_plan* plan;
+    unsigned long long used;  // call counter at the last use (least recently used is evicted)
+};
+// At most this many cached plans (each holds its carry slots, tables and launch state).
+constexpr size_t ONE_SHOT_CACHE_MAX = 32;
 std::mutex& cache_mu() {
     static std::mutex m;
     return m;
 }
-std::map<CacheKey, iir_plan*>& cache() {
-    static std::map<CacheKey, iir_plan*> c;
+std::map<CacheKey, CacheEntry>& cache() {
+    static std::map<CacheKey, CacheEntry> c;
     return c;
+}
+unsigned long long g_calls = 0;  // one-shot calls (LRU clock)
+int g_pending = IIR_OK;          // device failure of an evicted plan, returned by the next call
+long long g_debug_withhold = -1;  // iir_sos_filter_debug_withhold: chunk withheld by the next call
+long long g_debug_timeout_ns = 0;
+
+// Frees a cached plan once its device work has finished; a device failure it recorded becomes
+// the pending error of the one-shot API.
+void cache_drop(const CacheKey& key, iir_plan* p) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    if (cur != key.device) cudaSetDevice(key.device);
+    cudaDeviceSynchronize();
+    const int e = take_host_error(p);
+    if (e && g_pending == IIR_OK) g_pending = e;
+    plan_free(p);
+    if (cur != key.device) cudaSetDevice(cur);
 }
 }  // namespace
 
@@ -963,16 +1029,57 @@ extern "C" int iir_sos_filter_geom(const float* x, float* y, size_t n, const flo
     CacheKey key{device, stream, kernel, block_size, n_blocks, n_sections,
                  std::string(reinterpret_cast<const char*>(sos), sizeof(float) * 6 * n_sections)};
     std::lock_guard<std::mutex> lk(cache_mu());
+    // a device-side failure of an earlier call is returned first (that call's output is void)
+    if (g_pending != IIR_OK) {
+        st = g_pending;
+        g_pending = IIR_OK;
+        return st;
+    }
+    ++g_calls;
     auto it = cache().find(key);
     iir_plan* p = nullptr;
     if (it == cache().end()) {
+        if (cache().size() >= ONE_SHOT_CACHE_MAX) {
+            auto lru = cache().begin();
+            for (auto c = cache().begin(); c != cache().end(); ++c)
+                if (c->second.used < lru->second.used) lru = c;
+            cache_drop(lru->first, lru->second.plan);
+            cache().erase(lru);
+            if (g_pending != IIR_OK) {
+                st = g_pending;
+                g_pending = IIR_OK;
+                return st;
+            }
+        }
         st = iir_plan_create(&p, sos, n_sections, kernel, block_size, n_blocks, n);
         if (st) return st;
-        cache()[key] = p;
+        cache()[key] = CacheEntry{p, g_calls};
     } else {
-        p = it->second;
+        p = it->second.plan;
+        it->second.used = g_calls;
+        st = take_host_error(p);
+        if (st) return st;
+    }
+    if (g_debug_withhold >= 0) {
+        // fault injection for one launch: a withheld carry and a short wait limit
+        const long long keep = p->timeout_ns;
+        p->timeout_ns = g_debug_timeout_ns;
+        p->withhold = g_debug_withhold;
+        g_debug_withhold = -1;
+        st = iir_plan_execute(p, x, y, n, stream);
+        p->timeout_ns = keep;
+        p->withhold = -1;
+        return st;
     }
     return iir_plan_execute(p, x, y, n, stream);
+}
+
+extern "C" int iir_sos_filter_debug_withhold(long long chunk, long long timeout_ns) {
+    if (chunk < 0 || timeout_ns <= 0) return IIR_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(cache_mu());
+    g_debug_withhold = chunk;
+    g_debug_timeout_ns = timeout_ns;
+    return IIR_OK;
 }
 
 extern "C" int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_sections, int kernel,
@@ -982,8 +1089,9 @@ extern "C" int iir_sos_filter(const float* x, float* y, size_t n, const float* s
 
 extern "C" int iir_cache_clear(void) {
     std::lock_guard<std::mutex> lk(cache_mu());
-    cudaDeviceSynchronize();
-    for (auto& kv : cache()) plan_free(kv.second);
+    for (auto& kv : cache()) cache_drop(kv.first, kv.second.plan);
     cache().clear();
-    return IIR_OK;
+    const int st = g_pending;
+    g_pending = IIR_OK;
+    return st;
 }

@@ -33,6 +33,8 @@ bool encode_chunk_map(CUtensorMap* map, const float* base, long long n, int n_pe
                       bool planes);
 // cudaError_t -> IIR_* status (clears the runtime's sticky last error).
 int cuda_status(cudaError_t e);
+// A launch state's error word ((epoch << 32) | device code, 0 = none) -> IIR_* status.
+int device_error_status(unsigned long long word);
 
 // Precision form (iir_tc.cu): the cascade's chunk solve as tensor-core GEMMs.
 struct TcPlan;

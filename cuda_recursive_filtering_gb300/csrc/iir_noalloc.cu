@@ -7,10 +7,14 @@
 // and tables. This entry point keeps all three in one fixed array of static device memory
 // (g_scratch below) and launches the PH realization (32 x 64 geometry) on it.
 //
+// Each call launches two kernels on the caller's stream: na_prepare_kernel writes the filter's
+// lane tables into the array (the tables travel by value in its parameter block, so no host
+// buffer has to outlive the call), then the PH kernel filters.
+//
 // Limits: n <= IIR_NOALLOC_MAX_SAMPLES samples, 1..IIR_MAX_SECTIONS sections. The scratch
 // array is shared by every call on a device: calls must be ordered (one stream, or streams
 // ordered by events); calls that overlap in time race on the carry slots and produce wrong
-// output or a lookback timeout.
+// output or a lookback timeout. Such a device-side failure is returned by a later call.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -48,27 +52,85 @@ static_assert(NA_TABLE_BYTES % 256 == 0, "carry slots stay 256-byte aligned");
 static __device__ __align__(256) unsigned long long g_scratch[NA_BYTES / sizeof(unsigned long long)];
 
 constexpr int NA_MAX_DEVICES = 64;
+// Error words of the devices' launches, in host memory that the devices write to (page-locked
+// and mapped once, at the first setup): a failing launch stores its error word here, so a later
+// call sees it without synchronising. Static, so nothing is allocated for it.
+alignas(4096) unsigned long long g_host_err[4096 / sizeof(unsigned long long)];
+static_assert(NA_MAX_DEVICES <= 4096 / sizeof(unsigned long long), "one word per device");
+
 struct DeviceScratch {
     bool ready = false;
-    unsigned char* base = nullptr;
-    unsigned long long launches = 0;  // since the slots were last zeroed
+    unsigned char* base = nullptr;  // device address of g_scratch on this device
 };
 std::mutex g_mu;
 DeviceScratch g_dev[NA_MAX_DEVICES];
+std::once_flag g_register_once;
+int g_register_status = IIR_OK;
 
-// Once per device, with that device current: resolve the array's address and zero it.
+// Lane tables of up to NA_UPLOAD_SECTIONS sections, passed by value to na_prepare_kernel
+// (kernel parameters are limited to 32764 bytes).
+constexpr int NA_UPLOAD_SECTIONS = 4;
+struct NaUpload {
+    float4 tab[NA_UPLOAD_SECTIONS * IIR_TAB_STRIDE];
+    unsigned char* base;  // device address of g_scratch
+    int first;            // first section of this upload
+    int count;            // sections in it
+};
+static_assert(sizeof(NaUpload) <= 32000, "fits a kernel parameter block");
+
+constexpr int NA_PREP_THREADS = 512;
+
+// One block. The first upload of a call also restarts the launch-versioned state every 2^30
+// launches (the epoch is the launch count since the last restart): it zeroes the carry slots
+// and the ticket / error words, leaving the host error address in place. A single block does
+// it, so no other thread reads the state meanwhile; the filter launch that follows on the
+// stream sees epoch 0 and clean slots.
+__global__ void __launch_bounds__(NA_PREP_THREADS) na_prepare_kernel(const __grid_constant__ NaUpload u) {
+    IirLaunchState* state = reinterpret_cast<IirLaunchState*>(u.base);
+    if (u.first == 0) {
+        const unsigned long long t = *reinterpret_cast<volatile unsigned long long*>(&state->ticket);
+        if ((t >> 32) >= (1ull << 30)) {  // the same value in every thread: a uniform branch
+            unsigned long long* carry = reinterpret_cast<unsigned long long*>(u.base + NA_STATE_BYTES + NA_TABLE_BYTES);
+            for (size_t i = threadIdx.x; i < NA_CARRY_BYTES / sizeof(unsigned long long); i += blockDim.x) carry[i] = 0ull;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                state->ticket = 0ull;
+                state->error = 0ull;
+                state->done = 0u;
+            }
+        }
+    }
+    float4* tables = reinterpret_cast<float4*>(u.base + NA_STATE_BYTES) + static_cast<size_t>(u.first) * IIR_TAB_STRIDE;
+    for (int i = threadIdx.x; i < u.count * IIR_TAB_STRIDE; i += blockDim.x) tables[i] = u.tab[i];
+}
+
+// Once per device, with that device current: resolve the array's address, zero it and point
+// its launch state at the device's host error word.
 int setup(int device, DeviceScratch& d, const KernelEntry& e) {
     if (d.ready) return IIR_OK;
+    std::call_once(g_register_once, [] {
+        const cudaError_t r =
+            cudaHostRegister(g_host_err, sizeof(g_host_err), cudaHostRegisterMapped | cudaHostRegisterPortable);
+        g_register_status = (r == cudaSuccess || r == cudaErrorHostMemoryAlreadyRegistered) ? IIR_OK : cuda_status(r);
+        cudaGetLastError();
+    });
+    if (g_register_status) return g_register_status;
     void* ptr = nullptr;
     int st = cuda_status(cudaGetSymbolAddress(&ptr, g_scratch));
     if (st) return st;
     if (blocks_per_sm(e, device) <= 0) return IIR_ERR_UNSUPPORTED;
+    void* herr = nullptr;
+    st = cuda_status(cudaHostGetDevicePointer(&herr, &g_host_err[device], 0));
+    if (st) return st;
     st = cuda_status(cudaMemset(ptr, 0, NA_BYTES));
+    if (st) return st;
+    st = cuda_status(cudaMemcpy(static_cast<char*>(ptr) + offsetof(IirLaunchState, host_error), &herr, sizeof(herr),
+                                cudaMemcpyHostToDevice));
     if (st) return st;
     st = cuda_status(cudaDeviceSynchronize());
     if (st) return st;
+    g_host_err[device] = 0ull;
     d.base = static_cast<unsigned char*>(ptr);
-    d.launches = 0;
     d.ready = true;
     return IIR_OK;
 }
@@ -86,16 +148,19 @@ extern "C" int iir_sos_filter_noalloc(const float* x, float* y, size_t n, const 
     const KernelEntry* e = find_entry(IIR_KIND_PH, NA_B, NA_N, 0);
     if (!e || static_cast<size_t>(e->rows) * NA_N != NA_CHUNK) return IIR_ERR_UNSUPPORTED;
 
-    // coefficients and lane tables live on the host stack
+    // coefficients and lane tables, on the host stack; the tables reach the device by value in
+    // the parameter blocks of na_prepare_kernel
     SectionF32 secs[IIR_MAX_SECTIONS];
     double gain = 1.0;
     int st = normalise_sos(sos, n_sections, secs, gain);
     if (st) return st;
     IirParams q;
     std::memset(&q, 0, sizeof(q));
-    float4 tabs[IIR_TAB_STRIDE * IIR_MAX_SECTIONS];
+    NaUpload up[2];
     for (int s = 0; s < n_sections; ++s) {
-        st = precompute_section(secs[s], IIR_KIND_PH, e->rows, NA_N, q.sec[s], tabs + s * IIR_TAB_STRIDE);
+        NaUpload& u = up[s / NA_UPLOAD_SECTIONS];
+        st = precompute_section(secs[s], IIR_KIND_PH, e->rows, NA_N, q.sec[s],
+                                u.tab + (s % NA_UPLOAD_SECTIONS) * IIR_TAB_STRIDE);
         if (st) return st;
     }
 
@@ -107,23 +172,29 @@ extern "C" int iir_sos_filter_noalloc(const float* x, float* y, size_t n, const 
     DeviceScratch& d = g_dev[device];
     st = setup(device, d, *e);
     if (st) return st;
+    // a device-side failure of an earlier call on this device (its output is void)
+    volatile unsigned long long* herr = &g_host_err[device];
+    const unsigned long long failed = *herr;
+    if (failed) {
+        *herr = 0ull;
+        return device_error_status(failed);
+    }
     if (n == 0) return IIR_OK;
 
     cudaStream_t stream = static_cast<cudaStream_t>(stream_);
-    unsigned char* tables = d.base + NA_STATE_BYTES;
-    unsigned char* carry = tables + NA_TABLE_BYTES;
-    // Pageable source: the call returns once the driver has staged the bytes, so the stack
-    // buffer may go out of scope; the copy is ordered before the launch on the stream.
-    st = cuda_status(cudaMemcpyAsync(tables, tabs, sizeof(float4) * IIR_TAB_STRIDE * n_sections,
-                                     cudaMemcpyHostToDevice, stream));
-    if (st) return st;
-    if (++d.launches >= (1ull << 30)) {
-        st = cuda_status(cudaMemsetAsync(d.base, 0, NA_STATE_BYTES, stream));
-        if (!st) st = cuda_status(cudaMemsetAsync(carry, 0, NA_CARRY_BYTES, stream));
+    const int uploads = (n_sections + NA_UPLOAD_SECTIONS - 1) / NA_UPLOAD_SECTIONS;
+    for (int k = 0; k < uploads; ++k) {
+        up[k].base = d.base;
+        up[k].first = k * NA_UPLOAD_SECTIONS;
+        up[k].count = (n_sections - up[k].first < NA_UPLOAD_SECTIONS) ? n_sections - up[k].first : NA_UPLOAD_SECTIONS;
+        void* pargs[] = {&up[k]};
+        st = cuda_status(cudaLaunchKernel(reinterpret_cast<const void*>(na_prepare_kernel), dim3(1),
+                                          dim3(NA_PREP_THREADS), pargs, 0, stream));
         if (st) return st;
-        d.launches = 1;
     }
 
+    unsigned char* tables = d.base + NA_STATE_BYTES;
+    unsigned char* carry = tables + NA_TABLE_BYTES;
     const size_t nchunks = (n + NA_CHUNK - 1) / NA_CHUNK;
     q.x = x;
     q.y = y;

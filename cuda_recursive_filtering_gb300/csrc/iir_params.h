@@ -38,13 +38,18 @@
 // advances the epoch for the next launch (no per-block exit atomics; graph replays and
 // launches of different sizes stay consistent). Chunk order = ticket order = block start
 // order (the forward-progress argument of ph_kernels.cuh:227-229).
+// `host_error` is the device address of a word in host-mapped memory (or null): a failing
+// launch also stores its error word there, so the host can see a device-side failure of an
+// earlier launch without synchronising (the one-shot entry points report it on their next call).
+// Periodic re-zeroing covers the first IIR_STATE_RESET_BYTES only, never host_error.
 struct IirLaunchState {
     unsigned long long ticket;       // (epoch << 32) | ticket
     unsigned long long error;        // (epoch << 32) | status code of the first failure
     unsigned int done;               // persistent kernels: blocks of the launch that have exited
     unsigned int pad0;
-    unsigned long long pad[1];
+    unsigned long long* host_error;  // host-mapped error word, or null
 };
+#define IIR_STATE_RESET_BYTES 24  // ticket, error, done, pad0
 
 struct IirSection {
     float b1, b2;           // FIR taps after b0 normalisation (b0 = 1)

@@ -1349,7 +1349,7 @@ int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long tim
     }
     if (++t->launches >= (1ull << 30)) {
         int st = cuda_status(cudaMemsetAsync(t->d_carry, 0, t->carry_bytes, stream));
-        if (!st) st = cuda_status(cudaMemsetAsync(t->d_state, 0, sizeof(IirLaunchState), stream));
+        if (!st) st = cuda_status(cudaMemsetAsync(t->d_state, 0, IIR_STATE_RESET_BYTES, stream));
         if (st) return st;
         t->launches = 1;
     }

@@ -69,8 +69,14 @@ typedef struct iir_plan iir_plan;
  *   kernel     : IIR_KERNEL_*; block_size/n_blocks = 0 selects the tuned geometry.
  *   x, y       : device float32 arrays of n samples; they must not overlap.
  *   stream     : cudaStream_t. The call is stream-ordered; plans are cached internally
- *                per (device, stream, filter, kernel, geometry).
+ *                per (device, stream, filter, kernel, geometry), at most 32 of them (the least
+ *                recently used is freed, after a device synchronisation, to make room).
  * Zero initial state, as the reference (xi1/xi2/yi1/yi2 = 0, ph_kernels.cuh:162-165).
+ * Device-side failures (a lookback wait that ran out; the reference spins forever instead,
+ * ph_kernels.cuh:397-404) happen after the call has returned. They are reported, without a
+ * synchronisation, by a later call: the next call on the same cached plan returns
+ * IIR_ERR_LOOKBACK_TIMEOUT and launches nothing (the failed call's output is void), as does
+ * the next one-shot call after the failed plan was evicted, and iir_cache_clear.
  */
 int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_sections,
                    int kernel, void* stream);
@@ -87,12 +93,18 @@ int iir_sos_filter_geom(const float* x, float* y, size_t n, const float* sos, in
  * may fail under memory pressure, which a real-time caller (an audio or radio callback with a
  * deadline) or a caller whose device memory belongs to another allocator cannot accept.
  * Runs the PH realization (32 x 64) on one fixed static device array (about 2.2 MB per
- * device) that holds the launch state, the lane tables and the carry slots.
+ * device) that holds the launch state, the lane tables and the carry slots. Each call launches
+ * two kernels on `stream`: one that writes the filter's tables into the array (they travel in
+ * its parameter block) and the filter itself.
  *   - n <= IIR_NOALLOC_MAX_SAMPLES, else IIR_ERR_TOO_LARGE; 1 <= n_sections <= 8.
- *   - The first call on a device sets the array up (resolves its address, zeroes it,
- *     synchronises the device); make it before any stream capture.
+ *   - The first call on a device sets the array up (resolves its address, zeroes it, page-locks
+ *     a static host word that the device reports failures to, synchronises the device); make
+ *     it before any stream capture.
  *   - Every call on a device shares the array: calls must be ordered (one stream, or
- *     streams ordered by events). Calls that overlap in time race and give wrong output. */
+ *     streams ordered by events). Calls that overlap in time race and give wrong output.
+ *   - A device-side failure of a call (a lookback wait that ran out, as overlapping calls can
+ *     cause) is returned by a later call on the same device (IIR_ERR_LOOKBACK_TIMEOUT), which
+ *     then launches nothing; the failed call's output is void. */
 #define IIR_NOALLOC_MAX_SAMPLES (1ull << 26)
 int iir_sos_filter_noalloc(const float* x, float* y, size_t n, const float* sos, int n_sections,
                            void* stream);
@@ -195,8 +207,14 @@ int iir_batch_destroy(iir_batch* batch);
 const char* iir_status_string(int status);
 int iir_version(void);          /* major*10000 + minor*100 + patch */
 
-/* Drops every plan cached by iir_sos_filter (frees their device memory). */
+/* Drops every plan cached by iir_sos_filter (synchronises the device, frees their memory).
+ * Returns a device-side failure recorded by a cached plan and not yet reported, else IIR_OK. */
 int iir_cache_clear(void);
+
+/* Fault injection for tests of the one-shot error reporting: the next iir_sos_filter /
+ * iir_sos_filter_geom call withholds the carries of chunk `chunk` of its launch and waits at
+ * most `timeout_ns` for a predecessor (that launch only). No counterpart in the reference. */
+int iir_sos_filter_debug_withhold(long long chunk, long long timeout_ns);
 
 #ifdef __cplusplus
 }

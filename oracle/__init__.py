@@ -135,7 +135,7 @@ def errors(out, ref) -> dict:
 
 def passes_reference_gate(out, ref) -> bool:
     e = errors(out, ref)
-    return e["finite"] and e["rel_max"] <= REL_TOL_GATE
+    return e["finite"] and e["rel_max"] <= REF_REL_TOL
 
 
 REL_TOL_GATE = REF_REL_TOL
