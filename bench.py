@@ -359,20 +359,23 @@ def run_reference(args, rank: int, world: int) -> None:
 # forms (batching, serving, precision)
 # ------------------------------------------------------------------------------------------
 def run_batching(dev) -> dict:
-    """Many channels of uneven length, each with its own filter, in one launch (Batch.packed);
-    device-resident, CUDA events over 10 launches; a few channels checked against the oracle."""
+    """Many channels of uneven length, each with its own filter, in one persistent launch
+    (Batch.packed); the chunk shape chosen by autotune.tune_batch (every compiled shape timed, in
+    the order the occupancy model proposes); device-resident, CUDA events over 10 launches of the
+    chosen shape; a few channels checked against the oracle."""
     import numpy as np
     import torch
 
     import oracle
-    from cuda_recursive_filtering_gb300 import Batch, workloads
+    from cuda_recursive_filtering_gb300 import Batch, autotune, workloads
 
     filters, lens = workloads.multichannel_mixed()
-    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 8192 + len(filters)), device=dev)
+    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 1024 + len(filters)), device=dev)
     off = np.concatenate([[0], np.cumsum(lens)])
     x = workloads.uniform_signal(int(off[-1]), 3, device=dev)
     y = torch.empty_like(x)
     flt = np.arange(len(filters), dtype=np.int32)
+    tuned = autotune.tune_batch(batch, x, y, off, flt, reps=3)
     for _ in range(3):
         batch.packed(x, y, off, flt)
     torch.cuda.synchronize()
@@ -390,9 +393,10 @@ def run_batching(dev) -> dict:
         _, ref = oracle.reference_golden(filters[i], xi)
         worst = max(worst, oracle.errors(y[off[i]:off[i + 1]].cpu().numpy(), ref)["rel_max"])
     return {"workload": "4096 channels, lengths log-uniform [2^10, 2^20], own filter each: order {2,4,8,16}, "
-                        "butter / cheby1 (1 dB), cutoff U[0.02, 0.45], seed 3; one launch",
+                        "butter / cheby1 (1 dB), cutoff U[0.02, 0.45], seed 3; one persistent launch",
             "value": round(float(off[-1]) / (ms * 1e-3) / 1e9, 1), "unit": "GS/s", "ms_per_launch": ms,
-            "samples": int(off[-1]), "check_rel_max_8_channels": worst}
+            "samples": int(off[-1]), "check_rel_max_8_channels": worst, "shape": batch.shape(),
+            "tuner": tuned}
 
 
 def run_precision(dev, log2n: int, hbm_gbs: float) -> dict:
@@ -703,6 +707,28 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_only(args, spec: str) -> None:
+    """One realization / order / geometry on the plain workload at 2^LOG2N samples, timed like the
+    headline and nothing else (a short command to profile one kernel): spec = KERNEL:ORDER[:BxN]."""
+    import torch
+    from scipy import signal
+
+    import cuda_recursive_filtering_gb300 as pkg
+    from cuda_recursive_filtering_gb300 import Plan, workloads
+    parts = spec.split(":")
+    kernel, order = parts[0], int(parts[1])
+    b, nb = (int(v) for v in parts[2].split("x")) if len(parts) > 2 else (0, 0)
+    pkg.load_library()
+    dev = torch.device("cuda", 0)
+    n = 1 << LOG2N
+    x = workloads.uniform_signal(n, 1, device=dev)
+    y = torch.empty_like(x)
+    plan = Plan(signal.butter(order, 0.1, output="sos"), kernel, b, nb, max_n=n, device=dev)
+    ms = time_plan(plan, x, y, args.steps, args.warmup, torch.cuda.current_stream())
+    print(json.dumps({"only": spec, "plan": plan.info(), "n": n, "ms_per_launch": ms,
+                      "gsps": round(n / (ms * 1e-3) / 1e9, 1)}), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -714,6 +740,8 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
+    ap.add_argument("--only", default=None, metavar="KERNEL:ORDER[:BxN]",
+                    help="time one realization / order / geometry and print only that (for profiling)")
     args = ap.parse_args()
     globals()["LOG2N"] = args.log2n
     args.warmup = max(args.warmup, 3)
@@ -726,6 +754,8 @@ def main() -> None:
     try:
         if args.impl == "reference":
             run_reference(args, rank, world)
+        elif args.only:
+            run_only(args, args.only)
         else:
             run_ours(args, rank, world, local_rank)
     finally:

@@ -82,6 +82,8 @@ def load(path: str | None = None):
         "iir_batch_set_timeout_ns": ([vp, ll], i),
         "iir_batch_debug_withhold": ([vp, ll], i),
         "iir_batch_filter_sections": ([vp, i], i),
+        "iir_batch_set_shape": ([vp, i, i], i),
+        "iir_batch_get_shape": ([vp, ip, ip, ip, ip, ip, ip], i),
         "iir_batch_destroy": ([vp], i),
         "iir_batch_bind": ([vp, ctypes.POINTER(IirSegment), i, pp], i),
         "iir_batch_launch_bound": ([vp, vp], i),

@@ -221,6 +221,21 @@ class Batch:
     def state_size(self, filter_index: int) -> int:
         return 2 + 2 * self.n_sections[filter_index]
 
+    SHAPES = ((128, 64), (128, 32), (128, 16), (64, 16))  # rows x samples per row (compiled)
+
+    def set_shape(self, rows: int, samples_per_row: int) -> None:
+        """Chunk shape of later launches (C ABI: iir_batch_set_shape); one of SHAPES."""
+        check(self._lib.iir_batch_set_shape(self._ptr, int(rows), int(samples_per_row)), "iir_batch_set_shape")
+
+    def shape(self) -> dict:
+        """The current chunk shape: rows, samples_per_row, chunk, and its kernel's threads,
+        registers per thread, shared memory per block and resident blocks per SM."""
+        v = [ctypes.c_int() for _ in range(6)]
+        check(self._lib.iir_batch_get_shape(self._ptr, *[ctypes.byref(t) for t in v]), "iir_batch_get_shape")
+        r, n, th, rg, sm, b = (t.value for t in v)
+        return {"rows": r, "samples_per_row": n, "chunk": r * n, "threads": th, "regs_per_thread": rg,
+                "smem_bytes": sm, "blocks_per_sm": b}
+
     def __call__(self, segments, stream=None) -> None:
         arr = (_lib.IirSegment * max(1, len(segments)))()
         for i, seg in enumerate(segments):

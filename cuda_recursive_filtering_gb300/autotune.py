@@ -19,7 +19,8 @@ import torch
 
 from .api import Plan
 
-__all__ = ["tune", "tuned_plan"]
+__all__ = ["tune", "tuned_plan", "GB300", "supply_blocks_per_sm", "demand_blocks_per_sm", "rank_batch_shapes",
+           "tune_batch"]
 
 _CANDIDATES_ORDER2 = [("PH", 32, 64), ("PH", 32, 32), ("STCR_UNROLL", 32, 64), ("STCR_UNROLL", 32, 32),
                       ("DTCR_UNROLL", 32, 128), ("DTCR_UNROLL", 32, 64), ("PH", 32, 128), ("PLR", 0, 0)]
@@ -112,3 +113,98 @@ def tuned_plan(sos, n: int, **kw) -> Plan:
     """A Plan with the tuned realization and geometry for this filter and signal length."""
     best = tune(sos, n, **{k: v for k, v in kw.items() if k in ("candidates", "reps", "device", "cache_path")})
     return Plan(sos, best["kernel"], best["block_size"], best["n_blocks"], max_n=n, device=kw.get("device"))
+
+
+# ------------------------------------------------------------------------------------------------
+# Batching form: the chunk shape, chosen by timing, in the order an occupancy model proposes
+# ------------------------------------------------------------------------------------------------
+# The reference sizes its launches with an occupancy model of its two GPUs (gpu_specs.hpp:16-46 has
+# GTX 1070 and RTX 3060 profiles only, and compiling elsewhere silently uses the RTX 3060 one).
+# GB300 profile (sm_103a): 228 KB of shared memory per SM with 1 KB reserved per resident block,
+# 227 KB per block at most, 64 Ki registers, 2048 threads, 64 warps and 32 blocks per SM.
+GB300 = {"name": "GB300 (sm_103a)", "num_sms": 152, "registers_per_sm": 65536, "shared_mem_per_sm": 228 * 1024,
+         "reserved_shared_mem_per_tb": 1024, "max_shared_mem_per_tb": 227 * 1024, "max_threads_per_sm": 2048,
+         "max_warps_per_sm": 64, "max_tbs_per_sm": 32, "max_threads_per_tb": 1024, "warp_size": 32,
+         "register_alloc_unit": 256}
+
+
+def supply_blocks_per_sm(threads: int, regs_per_thread: int, smem_bytes: int, prof: dict = GB300) -> int:
+    """Resident blocks per SM the hardware allows (the supply side): gpu_specs.hpp:57-74
+    (compute_supply_tb_per_sm) restated with the kernel's own footprint instead of the
+    reference's estimate from BLOCK_SIZE x N_BLOCKS: the minimum over shared memory, registers
+    (allocated per warp in units of 256), threads, warps and the block cap."""
+    warps = -(-threads // prof["warp_size"])
+    unit = prof["register_alloc_unit"]
+    regs_per_warp = -(-regs_per_thread * prof["warp_size"] // unit) * unit
+    limits = [prof["shared_mem_per_sm"] // (smem_bytes + prof["reserved_shared_mem_per_tb"]),
+              prof["registers_per_sm"] // max(1, regs_per_warp * warps),
+              prof["max_threads_per_sm"] // threads,
+              prof["max_warps_per_sm"] // warps,
+              prof["max_tbs_per_sm"]]
+    return max(0, min(limits))
+
+
+def demand_blocks_per_sm(chunks: int, prof: dict = GB300) -> int:
+    """Blocks per SM the launch asks for when its chunks spread evenly over the SMs
+    (gpu_specs.hpp:83-86, compute_demand_tb_per_sm)."""
+    return -(-chunks // prof["num_sms"])
+
+
+def rank_batch_shapes(shapes: list[dict], lengths, prof: dict = GB300) -> list[dict]:
+    """Orders candidate chunk shapes for segments of the given lengths. For each shape, the
+    effective residency min(supply, demand) (gpu_specs.hpp:100-104) gives the samples in flight
+    per SM (residency x chunk), and the padding past every segment's end gives the fraction of the
+    launch's work that is useful. The score is useful fraction x in-flight samples, saturating at
+    the in-flight depth the largest shape reaches at full residency: work a chunk does not fill is
+    lost, and a shape that cannot keep enough samples in flight leaves HBM idle."""
+    lengths = np.asarray(lengths, dtype=np.int64)
+    total = int(lengths.sum())
+    rows = []
+    for sh in shapes:
+        chunk = sh["chunk"]
+        chunks = int(np.sum(-(-lengths // chunk)))
+        supply = supply_blocks_per_sm(sh["threads"], sh["regs_per_thread"], sh["smem_bytes"], prof)
+        resident = min(supply, demand_blocks_per_sm(chunks, prof))
+        rows.append(dict(sh, chunks=chunks, supply=supply, resident=resident,
+                         useful=total / max(1, chunks * chunk), in_flight=resident * chunk))
+    depth = max(r["supply"] * r["chunk"] for r in rows) or 1
+    for r in rows:
+        r["score"] = r["useful"] * min(1.0, r["in_flight"] / depth)
+    return sorted(rows, key=lambda r: -r["score"])
+
+
+def tune_batch(batch, x, y, offsets, filters, reps: int = 3, prof: dict | None = None) -> dict:
+    """Chooses the chunk shape of `batch` for segments packed in x / y at `offsets` (filters[i] for
+    segment i): every compiled shape, in the order rank_batch_shapes proposes, is timed over
+    `reps` launches (CUDA events, after one warm-up launch), and the fastest is left set.
+    Returns {"shape", "gsps", "table"} with the model's figures beside each measurement."""
+    from .api import Batch
+    prof = dict(GB300 if prof is None else prof)
+    prof["num_sms"] = torch.cuda.get_device_properties(batch.device).multi_processor_count
+    offsets = np.asarray(offsets, dtype=np.int64)
+    lengths = np.diff(offsets)
+    shapes = []
+    for rows_, n_ in Batch.SHAPES:
+        batch.set_shape(rows_, n_)
+        shapes.append(batch.shape())
+    table = []
+    for cand in rank_batch_shapes(shapes, lengths, prof):
+        batch.set_shape(cand["rows"], cand["samples_per_row"])
+        batch.packed(x, y, offsets, filters)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+        s.record()
+        for _ in range(reps):
+            batch.packed(x, y, offsets, filters)
+        e.record()
+        torch.cuda.synchronize()
+        batch.check()
+        ms = s.elapsed_time(e) / reps
+        table.append({k: cand[k] for k in ("rows", "samples_per_row", "chunk", "chunks", "supply", "resident",
+                                           "blocks_per_sm", "useful", "score")}
+                     | {"gsps": round(int(lengths.sum()) / (ms * 1e-3) / 1e9, 1)})
+    best = max(table, key=lambda t: t["gsps"])
+    batch.set_shape(best["rows"], best["samples_per_row"])
+    return {"shape": [best["rows"], best["samples_per_row"]], "gsps": best["gsps"], "table": table,
+            "model_order": [[t["rows"], t["samples_per_row"]] for t in table]}
+

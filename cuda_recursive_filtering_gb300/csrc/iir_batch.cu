@@ -1,19 +1,36 @@
-// iir_batch.cu — batched segments: many independent signals in one launch.
+// iir_batch.cu — batched segments: many independent signals in one persistent launch.
 //
 // A segment is one signal (a channel, or the next chunk of a live stream) with its own
 // cascade (any number of sections up to IIR_MAX_SECTIONS), an optional state in (zi) and an
 // optional state out (zf). The launch's chunks are the concatenation of every segment's
-// chunks; blocks take them in ticket order (one block per chunk, as iir_ph_kernel), find
-// their segment by binary search, and run the PH section solve (iir_ph.cuh) with the
-// decoupled lookback restricted to the segment: a segment's first chunk starts from zi, and
-// the lookback treats zi as the state before the segment. The block that holds a segment's
-// last sample writes zf. The reference filters one signal with one compile-time filter per
-// launch (ph_kernels.cuh:151-200, src/test_accuracy.cu:146); this is the batching form that
-// design cannot express.
+// chunks; that list is the launch's work queue. A persistent grid (every block resident: the
+// occupancy of the chosen kernel times the SMs) draws chunks from it in ticket order, one atomic
+// per chunk, finds each chunk's segment with a 32-way search of the segment start table, and
+// runs the PH section solve (iir_ph.cuh) with the decoupled lookback restricted to the segment:
+// a segment's first chunk starts from zi, and the lookback treats zi as the state before the
+// segment. The block that holds a segment's last sample writes zf. A chunk only ever waits for
+// a chunk drawn before it, which a running block holds, so the queue cannot deadlock.
+//
+// Each filter takes one of two schedules (chosen per filter when the chunk shape is set):
+//   * per-section lookback: each section publishes the chunk's zero-state aggregate and waits
+//     for its predecessor's (control(); two block barriers per section);
+//   * tail aggregate (iir_tail.cuh), when the filter's cascade state decays within half a chunk:
+//     the chunk's aggregate of every section comes from its last pieces, published at once; the
+//     chunk reads its predecessor's and the row warps run every section with one barrier each.
+//
+// The chunk shape (rows x samples per row) is a run-time choice among compiled instantiations
+// (iir_batch_set_shape): long channels favour big chunks (fewer lookbacks per sample), short ones
+// small chunks (less padding past a segment's end). The tuner in autotune.py picks it, seeded
+// by an occupancy model of GB300.
+//
+// The reference filters one signal with one compile-time filter per launch
+// (ph_kernels.cuh:151-200, src/test_accuracy.cu:146); this is the batching form that design
+// cannot express.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstddef>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -22,23 +39,34 @@
 #include "iir_host_internal.h"
 #include "iir_ph.cuh"
 #include "iir_registry.h"
+#include "iir_tail.cuh"
 
 namespace iirgb {
 
 struct BatchAux {
     unsigned int chunk, epoch, seg;
     int bail;
+    int more;  // the block drew a chunk of this launch
+    int pad[3];
     float wtot[16][2][2];
     float X[2];
+    float Xs[IIR_MAX_SECTIONS][2];                           // tail schedule: incoming states
+    float tpiece[IIR_TAIL_MAX_PIECES][IIR_MAX_SECTIONS][2];  // tail schedule: pieces' end states
 };
 
+template <int N_, int ROWS_>
 struct BatchBlock {
-    static constexpr int N = IIR_BATCH_N, ROWS = IIR_BATCH_ROWS, NW = ROWS / 32, THREADS = 32 + ROWS;
+    static constexpr int N = N_, ROWS = ROWS_, NW = ROWS / 32, THREADS = 32 + ROWS, WARPS = THREADS / 32;
     static constexpr int CHUNK = ROWS * N;
+    static_assert(ROWS % 32 == 0 && ROWS <= IIR_BATCH_MAX_ROWS, "rows per chunk");
     using Ph = PhBlock<32, N, ROWS>;
     static constexpr size_t SMEM_BYTES = CHUNK * sizeof(float) + sizeof(BatchAux) + 16;
+    // tail pieces a chunk of this shape takes: one per warp, at most half of the chunk
+    static constexpr int MAX_PIECES_RAW = WARPS < IIR_TAIL_MAX_PIECES ? WARPS : IIR_TAIL_MAX_PIECES;
+    static constexpr int MAX_PIECES = MAX_PIECES_RAW < CHUNK / (2 * IIR_TAIL_PIECE) ? MAX_PIECES_RAW
+                                                                                   : CHUNK / (2 * IIR_TAIL_PIECE);
 
-    // Incoming state of the segment's chunk lc for section `sec` (lookback within the segment).
+    // Per-section schedule: incoming state of the segment's chunk lc for section `sec`.
     __device__ static bool control(const IirBatchParams& p, BatchAux* aux, const IirBatchSegment& sg, int sec,
                                    uint32_t lc, uint32_t epoch, const float4* tab, float4 Gw) {
         const int lane = threadIdx.x & 31;
@@ -79,19 +107,18 @@ struct BatchBlock {
         return ok;
     }
 
-    __device__ static void run(const IirBatchParams& p, unsigned char* smem) {
-        float* buf = reinterpret_cast<float*>(smem);
-        BatchAux* aux = reinterpret_cast<BatchAux*>(smem + CHUNK * sizeof(float));
-        const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-        if (warp == 0) {
-            uint32_t epoch = 0, c = 0;
-            if (lane == 0) c = take_ticket(p.state, p.nchunks, epoch);
-            c = __shfl_sync(FULL_MASK, c, 0);
-            epoch = __shfl_sync(FULL_MASK, epoch, 0);
-            // segment holding chunk c: the last s with chunk_start[s] <= c (empty segments share
-            // their start with the next one, so the last such index is the non-empty one).
-            // 32-way search: each round the lanes probe 32 evenly spaced starts of [lo, hi).
-            uint32_t lo = 0, hi = p.nsegs;  // answer in [lo, hi)
+    // Warp 0: draws the block's next chunk from the launch's queue and finds its segment: the
+    // last s with chunk_start[s] <= c (empty segments share their start with the next one, so
+    // the last such index is the non-empty one). 32-way search: each round the lanes probe 32
+    // evenly spaced starts of [lo, hi).
+    __device__ static void draw(const IirBatchParams& p, BatchAux* aux, int lane) {
+        uint32_t c = 0;
+        if (lane == 0) c = static_cast<uint32_t>(atomicAdd(&p.state->ticket, 1ull) & 0xffffffffull);
+        c = __shfl_sync(FULL_MASK, c, 0);
+        const bool more = c < p.nchunks;
+        uint32_t lo = 0;
+        if (more) {
+            uint32_t hi = p.nsegs;  // answer in [lo, hi)
             while (hi - lo > 1) {
                 const uint32_t span = hi - lo;
                 const uint32_t probe = lo + static_cast<uint32_t>((static_cast<unsigned long long>(span) * lane) / 32);
@@ -104,14 +131,17 @@ struct BatchBlock {
                 lo = nlo;
                 hi = nhi > nlo ? nhi : nlo + 1;
             }
-            if (lane == 0) {
-                aux->chunk = c;
-                aux->epoch = epoch;
-                aux->seg = lo;
-                aux->bail = 0;
-            }
         }
-        __syncthreads();
+        if (lane == 0) {
+            aux->chunk = c;
+            aux->seg = lo;
+            aux->more = more ? 1 : 0;
+            aux->bail = 0;
+        }
+    }
+
+    // One chunk (all threads). Returns false when a wait of this launch gave up (uniform).
+    __device__ static bool chunk(const IirBatchParams& p, float* buf, BatchAux* aux, int tid, int warp, int lane) {
         const uint32_t c = aux->chunk, epoch = aux->epoch;
         const IirBatchSegment sg = p.segs[aux->seg];
         const IirBatchFilter flt = p.filters[sg.filter];
@@ -154,6 +184,39 @@ struct BatchBlock {
         __syncthreads();
 
         const bool row_warp = warp > 0;
+        const int K = flt.n_sections;
+        const bool tail = flt.tail > 0;  // the filter's schedule (uniform in the block)
+        if (tail) {
+            // the chunk's aggregate from its last pieces (not for the segment's last chunk)
+            const bool has_succ = nrem > CHUNK;
+            if (has_succ && warp < flt.tail) {
+                const TailFilter f{p.secs + flt.sec0, p.tables + static_cast<size_t>(flt.sec0) * IIR_BT_STRIDE,
+                                   IIR_BT_STRIDE, IIR_BT_TAIL, K, flt.gain};
+                tail_piece<N, ROWS, true>(f, flt.tail, buf, aux->tpiece, warp);
+            }
+            __syncthreads();  // the pieces are in aux; the staged chunk may now be changed
+            if (!row_warp) {
+                unsigned long long* slot = p.carry + static_cast<size_t>(sg.chunk0 + lc) * 4;  // section 0's
+                const uint32_t pf = 2u * epoch + 1u;
+                if (has_succ && static_cast<long long>(c) != p.withhold_chunk)
+                    tail_join_publish(p.phi + static_cast<size_t>(sg.filter) * IIR_BT_PHI_FLOATS, aux->tpiece, K,
+                                      flt.tail, slot, p.carry_stride, pf);
+                float X0 = 0.f, X1 = 0.f;
+                bool ok = true;
+                if (lc > 0) {
+                    ok = tail_poll(p, slot - 4, p.carry_stride, K, epoch, X0, X1);
+                } else if (sg.zi && lane < K) {
+                    X0 = sg.zi[2 + 2 * lane];  // the segment's initial state
+                    X1 = sg.zi[3 + 2 * lane];
+                }
+                if (lane < K) {
+                    aux->Xs[lane][0] = X0;
+                    aux->Xs[lane][1] = X1;
+                }
+                if (lane == 0) aux->bail = ok ? 0 : 1;
+            }
+        }
+
         const int w = warp - 1;
         const int r = w * 32 + lane;
         // A row warp whose rows all lie past the segment's end (padding of its last chunk) only
@@ -188,10 +251,11 @@ struct BatchBlock {
         // positions of the segment's last two samples relative to this chunk
         const long long m1 = nrem - 1, m2 = nrem - 2;  // in [0, CHUNK) when inside this chunk
         float pa1 = 0.f, pa2 = 0.f, d2 = 0.f, d1 = 0.f;
-        for (int sec = 0; sec < flt.n_sections; ++sec) {
+        for (int sec = 0; sec < K; ++sec) {
             const IirSection& q = p.secs[flt.sec0 + sec];
             const float4* tab = p.tables + static_cast<size_t>(flt.sec0 + sec) * IIR_BT_STRIDE;
             const float4 Gw = tab[IIR_BT_GPOW + 31];
+            const int wb = tail ? (sec & 1) : 0;  // the tail schedule alternates the totals' buffers
             float s0 = 0.f, s1 = 0.f, in0 = 0.f, in1 = 0.f;
             if (live) {
                 if (sec == 0)
@@ -201,25 +265,27 @@ struct BatchBlock {
                 warp_scan2<32, 1>(s0, s1, q.M, lane);
             }
             if (row_warp && lane == 31) {
-                aux->wtot[w][0][0] = s0;
-                aux->wtot[w][0][1] = s1;
+                aux->wtot[w][wb][0] = s0;
+                aux->wtot[w][wb][1] = s1;
             }
-            __syncthreads();  // (A)
+            // (A); with the tail schedule the control warp is done after the first section's
+            if (!tail || sec == 0) __syncthreads();
+            else if (row_warp) named_barrier_rows(NW);
             if (live) {
-                warp_incoming(aux, w, 0, Gw, in0, in1);
+                warp_incoming(aux, w, wb, Gw, in0, in1);
                 if (w > 0) {
                     float e0, e1;
                     mv2(tab[IIR_BT_GPOW + lane], in0, in1, e0, e1);
                     s0 += e0;
                     s1 += e1;
                 }
-            } else if (!row_warp) {
+            } else if (!row_warp && !tail) {
                 control(p, aux, sg, sec, lc, epoch, tab, Gw);
             }
-            __syncthreads();  // (B)
-            if (aux->bail) return;
+            if (!tail) __syncthreads();  // (B)
+            if (aux->bail) return false;
             if (live) {
-                const float X0 = aux->X[0], X1 = aux->X[1];
+                const float X0 = tail ? aux->Xs[sec][0] : aux->X[0], X1 = tail ? aux->Xs[sec][1] : aux->X[1];
                 float P0, P1;
                 mv2(tab[IIR_BT_CPOW + r], X0, X1, P0, P1);
                 const float T0 = s0 + P0, T1 = s1 + P1;
@@ -279,12 +345,32 @@ struct BatchBlock {
             sg.zf[1] = sg.x[sg.n - 1];
             sg.zf[0] = sg.n >= 2 ? sg.x[sg.n - 2] : (sg.zi ? sg.zi[1] : 0.f);
         }
+        return true;
+    }
+
+    // Persistent block: chunks from the launch's queue until it is empty (or a wait gave up);
+    // the last block to leave re-arms the queue for the next launch with the next epoch.
+    __device__ static void run(const IirBatchParams& p, unsigned char* smem) {
+        float* buf = reinterpret_cast<float*>(smem);
+        BatchAux* aux = reinterpret_cast<BatchAux*>(smem + CHUNK * sizeof(float));
+        const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+        if (tid == 0)  // tickets only add to the low word within a launch: the high word is the epoch
+            aux->epoch = static_cast<uint32_t>(*reinterpret_cast<volatile unsigned long long*>(&p.state->ticket) >> 32);
+        while (true) {
+            if (warp == 0) draw(p, aux, lane);
+            __syncthreads();
+            if (!aux->more) break;
+            if (!chunk(p, buf, aux, tid, warp, lane)) break;
+        }
+        __syncthreads();
+        if (tid == 0) pipe_finish(p.state, aux->epoch);
     }
 };
 
-__global__ void __launch_bounds__(BatchBlock::THREADS, 6) iir_batch_kernel(const __grid_constant__ IirBatchParams p) {
+template <int N, int ROWS>
+__global__ void __launch_bounds__(BatchBlock<N, ROWS>::THREADS, 4) iir_batch_kernel(const __grid_constant__ IirBatchParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    BatchBlock::run(p, smem);
+    BatchBlock<N, ROWS>::run(p, smem);
 }
 
 }  // namespace iirgb
@@ -295,13 +381,56 @@ __global__ void __launch_bounds__(BatchBlock::THREADS, 6) iir_batch_kernel(const
 using namespace iirgb;
 using namespace iirhost;
 
+namespace {
+
+// A compiled chunk shape of the batch kernel.
+struct ShapeDef {
+    int rows, n;
+    const void* fn;
+    int threads;
+    size_t smem;
+    int max_pieces;
+};
+
+template <int N, int ROWS>
+ShapeDef shape_def() {
+    using Blk = BatchBlock<N, ROWS>;
+    return ShapeDef{ROWS, N, reinterpret_cast<const void*>(iir_batch_kernel<N, ROWS>), Blk::THREADS, Blk::SMEM_BYTES,
+                    Blk::MAX_PIECES};
+}
+
+// chunks of 8192, 4096, 2048 and 1024 samples (the first is the default)
+const std::vector<ShapeDef>& shapes() {
+    static const std::vector<ShapeDef> s = {shape_def<64, 128>(), shape_def<32, 128>(), shape_def<16, 128>(),
+                                            shape_def<16, 64>()};
+    return s;
+}
+
+// Per-shape device data: lane tables of every section and the filters (with each filter's
+// schedule for this shape), built when the shape is first used; the occupancy of its kernel.
+struct ShapeData {
+    bool ready = false;
+    float4* d_tables = nullptr;
+    IirBatchFilter* d_filters = nullptr;
+    int blocks_per_sm = 0;
+    int regs = 0;  // registers per thread of the shape's kernel
+};
+
+}  // namespace
+
 struct iir_batch {
     int device = 0;
+    int sms = 0;
     int n_filters = 0;
     int max_sections = 0;
-    IirBatchFilter* d_filters = nullptr;
+    // filters on the host: normalised sections, gains, sections per filter, tail pieces needed
+    std::vector<SectionF32> sec32;
+    std::vector<IirBatchFilter> filters;
+    std::vector<int> tail_need;  // least number of tail pieces for the filter's state to decay (0: > 8)
     IirSection* d_secs = nullptr;
-    float4* d_tables = nullptr;
+    float* d_phi = nullptr;
+    std::vector<ShapeData> shape_data;
+    int shape = 0;  // index into shapes()
     IirLaunchState* d_state = nullptr;
     unsigned long long* d_carry = nullptr;
     size_t carry_cap = 0, gcap = 0, carry_bytes = 0;
@@ -354,7 +483,7 @@ int batch_alloc_carry(iir_batch* b, size_t chunks, size_t segs) {
     const size_t bytes = words * sizeof(unsigned long long) * static_cast<size_t>(b->max_sections);
     int st = cuda_status(cudaMalloc(&b->d_carry, bytes));
     if (!st) st = cuda_status(cudaMemset(b->d_carry, 0, bytes));
-    if (!st) st = cuda_status(cudaMemset(b->d_state, 0, sizeof(IirLaunchState)));
+    if (!st) st = cuda_status(cudaMemset(b->d_state, 0, IIR_STATE_RESET_BYTES));
     if (st) return st;
     b->carry_cap = chunks;
     b->gcap = gcap;
@@ -369,12 +498,108 @@ void batch_free(iir_batch* b) {
     batch_free_segments(b);
     for (int i = 0; i < 2; ++i)
         if (b->stage_done[i]) cudaEventDestroy(b->stage_done[i]);
-    if (b->d_filters) cudaFree(b->d_filters);
+    for (ShapeData& d : b->shape_data) {
+        if (d.d_tables) cudaFree(d.d_tables);
+        if (d.d_filters) cudaFree(d.d_filters);
+    }
     if (b->d_secs) cudaFree(b->d_secs);
-    if (b->d_tables) cudaFree(b->d_tables);
+    if (b->d_phi) cudaFree(b->d_phi);
     if (b->d_state) cudaFree(b->d_state);
     if (b->d_carry) cudaFree(b->d_carry);
     delete b;
+}
+
+// Tail-aggregate schedule for batched filters (IIR_GB300_TAIL=0 turns it off, as for plans).
+bool batch_tail_enabled() {
+    if (std::getenv("IIR_GB300_FULL_LOOKBACK")) return false;
+    const char* e = std::getenv("IIR_GB300_TAIL");
+    return !(e && std::atoi(e) == 0);
+}
+
+// Builds shape k's lane tables and filter records (once) and its occupancy.
+int shape_prepare(iir_batch* b, int k) {
+    ShapeData& d = b->shape_data[static_cast<size_t>(k)];
+    if (d.ready) return IIR_OK;
+    const ShapeDef& sd = shapes()[static_cast<size_t>(k)];
+    std::vector<float4> tabs(b->sec32.size() * IIR_BT_STRIDE, make_float4(0, 0, 0, 0));
+    std::vector<float4> full(IIR_TAB_STRIDE);
+    for (size_t s = 0; s < b->sec32.size(); ++s) {
+        IirSection q;
+        const int st = precompute_section(b->sec32[s], IIR_KIND_PH, sd.rows, sd.n, q, full.data());
+        if (st) return st;
+        float4* t = tabs.data() + s * IIR_BT_STRIDE;
+        for (int r = 0; r < sd.rows; ++r) t[IIR_BT_CPOW + r] = full[IIR_TAB_CPOW + r];
+        for (int i = 0; i < 32; ++i) t[IIR_BT_GPOW + i] = full[IIR_TAB_GPOW + i];
+        for (int l = 0; l <= 32; ++l) {
+            t[IIR_BT_QC + l] = full[IIR_TAB_QC + l];
+            t[IIR_BT_QG + l] = full[IIR_TAB_QG + l];
+        }
+        t[IIR_BT_LBD] = full[IIR_TAB_LBD];
+        for (int l = 0; l < 32; ++l) t[IIR_BT_TAIL + l] = full[IIR_TAB_TAIL + l];
+    }
+    std::vector<IirBatchFilter> flt = b->filters;
+    const bool tail_on = batch_tail_enabled();
+    for (size_t f = 0; f < flt.size(); ++f) {
+        const int need = b->tail_need[f];
+        flt[f].tail = (tail_on && need > 0 && need <= sd.max_pieces) ? need : 0;
+    }
+    int st = cuda_status(cudaMalloc(&d.d_tables, tabs.size() * sizeof(float4)));
+    if (!st) st = cuda_status(cudaMemcpy(d.d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (!st) st = cuda_status(cudaMalloc(&d.d_filters, flt.size() * sizeof(IirBatchFilter)));
+    if (!st)
+        st = cuda_status(cudaMemcpy(d.d_filters, flt.data(), flt.size() * sizeof(IirBatchFilter), cudaMemcpyHostToDevice));
+    if (!st)
+        st = cuda_status(
+            cudaFuncSetAttribute(sd.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sd.smem)));
+    if (!st) st = cuda_status(cudaFuncSetAttribute(sd.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int nb = 0;
+    if (!st) st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sd.fn, sd.threads, sd.smem));
+    cudaFuncAttributes fa{};
+    if (!st) st = cuda_status(cudaFuncGetAttributes(&fa, sd.fn));
+    if (st) return st;
+    if (nb <= 0) return IIR_ERR_UNSUPPORTED;
+    d.blocks_per_sm = nb;
+    d.regs = fa.numRegs;
+    d.ready = true;
+    return IIR_OK;
+}
+
+// Parameters of a launch over `nchunks` chunks with shape k (segment tables already on the device).
+IirBatchParams batch_params(const iir_batch* b, int k, const IirBatchSegment* segs, const unsigned int* starts,
+                            unsigned int nsegs, unsigned int nchunks, long long withhold) {
+    IirBatchParams q{};
+    q.segs = segs;
+    q.chunk_start = starts;
+    q.filters = b->shape_data[static_cast<size_t>(k)].d_filters;
+    q.secs = b->d_secs;
+    q.tables = b->shape_data[static_cast<size_t>(k)].d_tables;
+    q.phi = b->d_phi;
+    q.carry = b->d_carry;
+    q.state = b->d_state;
+    q.carry_stride = 4 * (b->carry_cap + b->gcap);
+    q.timeout_ns = b->timeout_ns;
+    q.withhold_chunk = withhold;
+    q.nsegs = nsegs;
+    q.nchunks = nchunks;
+    q.carry_cap = static_cast<unsigned int>(b->carry_cap);
+    q.max_sections = b->max_sections;
+    return q;
+}
+
+// The persistent launch: at most every resident block of shape k's kernel.
+int batch_launch(const iir_batch* b, int k, IirBatchParams& q, cudaStream_t stream) {
+    const ShapeDef& sd = shapes()[static_cast<size_t>(k)];
+    const size_t resident = static_cast<size_t>(b->shape_data[static_cast<size_t>(k)].blocks_per_sm) * b->sms;
+    const unsigned grid = static_cast<unsigned>(std::min<size_t>(q.nchunks, resident));
+    void* args[] = {&q};
+    return cuda_status(cudaLaunchKernel(sd.fn, dim3(grid), dim3(sd.threads), args, sd.smem, stream));
+}
+
+// chunks of a segment of n samples with shape k
+size_t seg_chunks(size_t n, int k) {
+    const ShapeDef& sd = shapes()[static_cast<size_t>(k)];
+    const size_t chunk = static_cast<size_t>(sd.rows) * sd.n;
+    return (n + chunk - 1) / chunk;
 }
 
 }  // namespace
@@ -385,60 +610,62 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
                      size_t max_chunks) {
     if (!out || !sos || !n_sections || n_filters < 1) return IIR_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    std::vector<IirBatchFilter> filters(static_cast<size_t>(n_filters));
+    iir_batch* b = new iir_batch();
+    b->n_filters = n_filters;
+    b->filters.resize(static_cast<size_t>(n_filters));
+    b->tail_need.assign(static_cast<size_t>(n_filters), 0);
     std::vector<IirSection> secs;
-    std::vector<float4> tabs;
+    std::vector<float> phi(static_cast<size_t>(n_filters) * IIR_BT_PHI_FLOATS, 0.f);
     std::vector<float4> full(IIR_TAB_STRIDE);
+    const ShapeDef& sd0 = shapes()[0];
     int max_sec = 1;
     size_t off = 0;
     for (int f = 0; f < n_filters; ++f) {
         const int ns = n_sections[f];
-        if (ns < 1 || ns > IIR_MAX_SECTIONS) return IIR_ERR_INVALID_ARGUMENT;
+        if (ns < 1 || ns > IIR_MAX_SECTIONS) {
+            delete b;
+            return IIR_ERR_INVALID_ARGUMENT;
+        }
         SectionF32 s32[IIR_MAX_SECTIONS];
         double gain = 1.0;
         int st = normalise_sos(sos + 6 * off, ns, s32, gain);
-        if (st) return st;
-        filters[f] = IirBatchFilter{static_cast<float>(gain), ns, static_cast<int>(secs.size()), 0};
+        if (st) {
+            delete b;
+            return st;
+        }
+        b->filters[static_cast<size_t>(f)] = IirBatchFilter{static_cast<float>(gain), ns, static_cast<int>(secs.size()), 0};
         for (int k = 0; k < ns; ++k) {
             IirSection q;
-            st = precompute_section(s32[k], IIR_KIND_PH, IIR_BATCH_ROWS, IIR_BATCH_N, q, full.data());
-            if (st) return st;
-            secs.push_back(q);
-            const size_t base = tabs.size();
-            tabs.resize(base + IIR_BT_STRIDE, make_float4(0, 0, 0, 0));
-            for (int r = 0; r < IIR_BATCH_ROWS; ++r) tabs[base + IIR_BT_CPOW + r] = full[IIR_TAB_CPOW + r];
-            for (int t = 0; t < 32; ++t) tabs[base + IIR_BT_GPOW + t] = full[IIR_TAB_GPOW + t];
-            for (int l = 0; l <= 32; ++l) {
-                tabs[base + IIR_BT_QC + l] = full[IIR_TAB_QC + l];
-                tabs[base + IIR_BT_QG + l] = full[IIR_TAB_QG + l];
+            st = precompute_section(s32[k], IIR_KIND_PH, sd0.rows, sd0.n, q, full.data());
+            if (st) {
+                delete b;
+                return st;
             }
-            tabs[base + IIR_BT_LBD] = full[IIR_TAB_LBD];
+            secs.push_back(q);
+            b->sec32.push_back(s32[k]);
         }
+        // tail-aggregate schedule: pieces for the cascade's state to decay, and Phi^512
+        std::vector<float> pf;
+        b->tail_need[static_cast<size_t>(f)] = tail_pieces(s32, ns, IIR_TAIL_MAX_PIECES, pf);
+        std::copy(pf.begin(), pf.end(), phi.begin() + static_cast<size_t>(f) * IIR_BT_PHI_FLOATS);
         max_sec = std::max(max_sec, ns);
         off += static_cast<size_t>(ns);
     }
-    iir_batch* b = new iir_batch();
-    b->n_filters = n_filters;
     b->max_sections = max_sec;
     b->filter_sections.assign(n_sections, n_sections + n_filters);
+    b->shape_data.resize(shapes().size());
     int st = cuda_status(cudaGetDevice(&b->device));
-    if (!st) st = cuda_status(cudaMalloc(&b->d_filters, filters.size() * sizeof(IirBatchFilter)));
+    if (!st) st = cuda_status(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
     if (!st) st = cuda_status(cudaMalloc(&b->d_secs, secs.size() * sizeof(IirSection)));
-    if (!st) st = cuda_status(cudaMalloc(&b->d_tables, tabs.size() * sizeof(float4)));
-    if (!st)
-        st = cuda_status(cudaMemcpy(b->d_filters, filters.data(), filters.size() * sizeof(IirBatchFilter),
-                                    cudaMemcpyHostToDevice));
     if (!st) st = cuda_status(cudaMemcpy(b->d_secs, secs.data(), secs.size() * sizeof(IirSection), cudaMemcpyHostToDevice));
-    if (!st)
-        st = cuda_status(cudaMemcpy(b->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (!st) st = cuda_status(cudaMalloc(&b->d_phi, phi.size() * sizeof(float)));
+    if (!st) st = cuda_status(cudaMemcpy(b->d_phi, phi.data(), phi.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (!st) st = cuda_status(cudaMalloc(&b->d_state, sizeof(IirLaunchState)));
+    if (!st) st = cuda_status(cudaMemset(b->d_state, 0, sizeof(IirLaunchState)));
     if (!st) st = batch_alloc_segments(b, max_segments);
     if (!st) st = batch_alloc_carry(b, max_chunks, b->seg_cap);
     for (int i = 0; i < 2 && !st; ++i) st = cuda_status(cudaEventCreateWithFlags(&b->stage_done[i], cudaEventDisableTiming));
-    if (!st)
-        st = cuda_status(cudaFuncSetAttribute(reinterpret_cast<const void*>(iir_batch_kernel),
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(BatchBlock::SMEM_BYTES)));
+    if (!st) st = shape_prepare(b, 0);
     if (st) {
         batch_free(b);
         return st;
@@ -447,9 +674,37 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
     return IIR_OK;
 }
 
+int iir_batch_set_shape(iir_batch* b, int rows, int samples_per_row) {
+    if (!b) return IIR_ERR_INVALID_ARGUMENT;
+    for (size_t k = 0; k < shapes().size(); ++k) {
+        if (shapes()[k].rows == rows && shapes()[k].n == samples_per_row) {
+            const int st = shape_prepare(b, static_cast<int>(k));
+            if (st) return st;
+            b->shape = static_cast<int>(k);
+            return IIR_OK;
+        }
+    }
+    return IIR_ERR_UNSUPPORTED;
+}
+
+int iir_batch_get_shape(const iir_batch* b, int* rows, int* samples_per_row, int* threads, int* regs_per_thread,
+                        int* smem_bytes, int* blocks_per_sm) {
+    if (!b) return IIR_ERR_INVALID_ARGUMENT;
+    const ShapeDef& sd = shapes()[static_cast<size_t>(b->shape)];
+    const ShapeData& d = b->shape_data[static_cast<size_t>(b->shape)];
+    if (rows) *rows = sd.rows;
+    if (samples_per_row) *samples_per_row = sd.n;
+    if (threads) *threads = sd.threads;
+    if (regs_per_thread) *regs_per_thread = d.regs;
+    if (smem_bytes) *smem_bytes = static_cast<int>(sd.smem);
+    if (blocks_per_sm) *blocks_per_sm = d.blocks_per_sm;
+    return IIR_OK;
+}
+
 int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* stream_) {
     if (!b || n_segs < 0 || (n_segs > 0 && !segs)) return IIR_ERR_INVALID_ARGUMENT;
     cudaStream_t stream = static_cast<cudaStream_t>(stream_);
+    const int k = b->shape;
     // validate and count chunks
     size_t total = 0, groups = 0;
     for (int i = 0; i < n_segs; ++i) {
@@ -460,7 +715,7 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
         const char* xb = reinterpret_cast<const char*>(s.x);
         const char* yb = reinterpret_cast<const char*>(s.y);
         if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
-        const size_t ch = (s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK;
+        const size_t ch = seg_chunks(s.n, k);
         total += ch;
         groups += (ch + IIR_GROUP - 1) / IIR_GROUP;
     }
@@ -492,7 +747,7 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
     unsigned int chunk0 = 0, group0 = 0;
     for (int i = 0; i < n_segs; ++i) {
         const iir_segment& s = segs[i];
-        const unsigned int ch = static_cast<unsigned int>((s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK);
+        const unsigned int ch = static_cast<unsigned int>(seg_chunks(s.n, k));
         hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, chunk0, group0, s.filter, 0};
         hstart[i] = chunk0;
         chunk0 += ch;
@@ -505,29 +760,15 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
                                          cudaMemcpyHostToDevice, stream));
     if (!st) st = cuda_status(cudaEventRecord(b->stage_done[turn], stream));
     if (st) return st;
-    IirBatchParams q{};
-    q.segs = b->d_segs;
-    q.chunk_start = b->d_starts;
-    q.filters = b->d_filters;
-    q.secs = b->d_secs;
-    q.tables = b->d_tables;
-    q.carry = b->d_carry;
-    q.state = b->d_state;
-    q.carry_stride = 4 * (b->carry_cap + b->gcap);
-    q.timeout_ns = b->timeout_ns;
-    q.withhold_chunk = b->withhold;
-    q.nsegs = static_cast<unsigned int>(n_segs);
-    q.nchunks = static_cast<unsigned int>(total);
-    q.carry_cap = static_cast<unsigned int>(b->carry_cap);
-    q.max_sections = b->max_sections;
+    IirBatchParams q = batch_params(b, k, b->d_segs, b->d_starts, static_cast<unsigned int>(n_segs),
+                                    static_cast<unsigned int>(total), b->withhold);
     b->withhold = -1;
-    void* args[] = {&q};
-    return cuda_status(cudaLaunchKernel(reinterpret_cast<const void*>(iir_batch_kernel), dim3(static_cast<unsigned>(total)),
-                                        dim3(BatchBlock::THREADS), args, BatchBlock::SMEM_BYTES, stream));
+    return batch_launch(b, k, q, stream);
 }
 
 struct iir_batch_bound {
     iir_batch* b = nullptr;
+    int shape = 0;
     IirBatchSegment* d_segs = nullptr;
     unsigned int* d_starts = nullptr;
     IirBatchParams params{};
@@ -537,6 +778,7 @@ struct iir_batch_bound {
 int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_bound** out) {
     if (!b || !out || n_segs < 0 || (n_segs > 0 && !segs)) return IIR_ERR_INVALID_ARGUMENT;
     *out = nullptr;
+    const int k = b->shape;
     std::vector<IirBatchSegment> hs(static_cast<size_t>(std::max(n_segs, 1)));
     std::vector<unsigned int> starts(static_cast<size_t>(n_segs) + 1);
     size_t chunk0 = 0, group0 = 0;
@@ -548,7 +790,7 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
         const char* xb = reinterpret_cast<const char*>(s.x);
         const char* yb = reinterpret_cast<const char*>(s.y);
         if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
-        const size_t ch = (s.n + BatchBlock::CHUNK - 1) / BatchBlock::CHUNK;
+        const size_t ch = seg_chunks(s.n, k);
         hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, static_cast<unsigned int>(chunk0),
                                 static_cast<unsigned int>(group0), s.filter, 0};
         starts[i] = static_cast<unsigned int>(chunk0);
@@ -565,6 +807,7 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
     }
     iir_batch_bound* h = new iir_batch_bound();
     h->b = b;
+    h->shape = k;
     h->nchunks = static_cast<unsigned int>(chunk0);
     st = cuda_status(cudaMalloc(&h->d_segs, hs.size() * sizeof(IirBatchSegment)));
     if (!st) st = cuda_status(cudaMalloc(&h->d_starts, starts.size() * sizeof(unsigned int)));
@@ -579,21 +822,7 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
         delete h;
         return st;
     }
-    IirBatchParams& q = h->params;
-    q.segs = h->d_segs;
-    q.chunk_start = h->d_starts;
-    q.filters = b->d_filters;
-    q.secs = b->d_secs;
-    q.tables = b->d_tables;
-    q.carry = b->d_carry;
-    q.state = b->d_state;
-    q.carry_stride = 4 * (b->carry_cap + b->gcap);
-    q.timeout_ns = b->timeout_ns;
-    q.withhold_chunk = -1;
-    q.nsegs = static_cast<unsigned int>(n_segs);
-    q.nchunks = h->nchunks;
-    q.carry_cap = static_cast<unsigned int>(b->carry_cap);
-    q.max_sections = b->max_sections;
+    h->params = batch_params(b, k, h->d_segs, h->d_starts, static_cast<unsigned int>(n_segs), h->nchunks, -1);
     *out = h;
     return IIR_OK;
 }
@@ -611,9 +840,7 @@ int iir_batch_launch_bound(iir_batch_bound* h, void* stream_) {
         if (st) return st;
         b->launches = 1;
     }
-    void* args[] = {&h->params};
-    return cuda_status(cudaLaunchKernel(reinterpret_cast<const void*>(iir_batch_kernel), dim3(h->nchunks),
-                                        dim3(BatchBlock::THREADS), args, BatchBlock::SMEM_BYTES, stream));
+    return batch_launch(b, h->shape, h->params, stream);
 }
 
 int iir_batch_unbind(iir_batch_bound* h) {
@@ -637,8 +864,7 @@ int iir_batch_check(iir_batch* b, void* stream_) {
     const unsigned long long zero = 0ull;
     cudaMemcpy(reinterpret_cast<char*>(b->d_state) + offsetof(IirLaunchState, error), &zero, sizeof(zero),
                cudaMemcpyHostToDevice);
-    const unsigned code = static_cast<unsigned>(hs.error & 0xffffffffull);
-    return code == IIR_DEV_ERR_TIMEOUT ? IIR_ERR_LOOKBACK_TIMEOUT : IIR_ERR_CUDA;
+    return device_error_status(hs.error);
 }
 
 int iir_batch_set_timeout_ns(iir_batch* b, long long timeout_ns) {

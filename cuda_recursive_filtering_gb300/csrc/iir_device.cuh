@@ -469,8 +469,12 @@ struct BlockAux {
     unsigned int epoch;
     int bail;
     int pad;
-    float wtot[16][2][2];  // per row warp, per scan q: zero-state warp totals
+    float wtot[16][2][2];  // per row warp, per scan q (tail schedule: per section parity): zero-state warp totals
     float X[2];            // lookback result (incoming state of the chunk)
+    float Xs[IIR_MAX_SECTIONS][2];    // tail schedule: incoming state of the chunk, every section
+    float tpiece[IIR_TAIL_MAX_PIECES][IIR_MAX_SECTIONS][2];  // tail schedule: pieces' end states
+    float xch[2][16][2];    // cyclic-reduction tiles over several warps: per-level row hand-off
+    float xscan[16][2][2];  // and the warps' top-level scan totals
 };
 
 // Occupancy target of the row-major kernels (registers left for the lookback's state).

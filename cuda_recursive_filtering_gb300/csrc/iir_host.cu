@@ -51,15 +51,25 @@ std::vector<KernelEntry>& registry() {
     return reg;
 }
 
-const KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline) {
+const KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline, int tail) {
     for (const KernelEntry& e : registry())
-        if (e.kind == kind && e.B == B && e.N == N && e.order == order && e.pipeline == pipeline) return &e;
+        if (e.kind == kind && e.B == B && e.N == N && e.order == order && e.pipeline == pipeline && e.tail == tail)
+            return &e;
     return nullptr;
 }
 
 // Schedule of single-section filters: the persistent pipeline where one is registered for
 // the realization and geometry, unless IIR_GB300_SCHEDULE=ticket asks for the one-block-per-
 // chunk kernel (kept for comparison).
+// Tail-aggregate schedule for cascades: at most this many IIR_TAIL_PIECE-sample pieces in a
+// chunk's tail (IIR_GB300_TAIL=<pieces>; 0 keeps the per-section lookback everywhere). The
+// planner also keeps it within one piece per warp of the block and half of the chunk.
+int tail_max_pieces() {  // read when a plan is created
+    if (std::getenv("IIR_GB300_FULL_LOOKBACK")) return 0;  // the exact per-section lookback everywhere
+    const char* e = std::getenv("IIR_GB300_TAIL");
+    return e ? std::max(0, std::atoi(e)) : IIR_TAIL_MAX_PIECES;
+}
+
 bool pipeline_enabled() {
     static const bool on = [] {
         const char* v = std::getenv("IIR_GB300_SCHEDULE");
@@ -222,6 +232,15 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
     }
     for (int l = IIR_TAB_QG + 33; l < IIR_TAB_STRIDE; ++l) tab[l] = make_float4(0, 0, 0, 0);
     tab[IIR_TAB_HALF] = to_f4(mpow(A, static_cast<unsigned long long>(N / 2)));
+    // tail-aggregate schedule: (A^16)^(l+1) for lanes of IIR_TAIL_PIECE / 32 = 16 samples
+    {
+        const M2 Al = mpow(A, static_cast<unsigned long long>(IIR_TAIL_PIECE / 32));
+        M2 Pt = Al;
+        for (int l = 0; l < 32; ++l) {
+            tab[IIR_TAB_TAIL + l] = to_f4(Pt);
+            Pt = mmul(Pt, Al);
+        }
+    }
     // truncated lookback: the least m <= 4 with ||Q^m||_inf <= 1e-10 (a chunk's incoming state
     // is then the sum of its m predecessors' aggregates to that bound), else 0
     {
@@ -236,6 +255,57 @@ int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSectio
         tab[IIR_TAB_LBD] = make_float4(static_cast<float>(depth), 0.f, 0.f, 0.f);
     }
     return IIR_OK;
+}
+
+// Tail-aggregate schedule (iir_tail.cuh): the least number P of IIR_TAIL_PIECE-sample pieces
+// with ||Phi^(IIR_TAIL_PIECE P)||_inf <= 1e-10, where Phi is the cascade's one-sample transition
+// of the state (y_s[n-2], y_s[n-1]) of every section s with zero input (section s > 0 also sees
+// its predecessor's new output and history through its FIR taps); FP64 from the float32
+// coefficients. 0 if P would exceed max_pieces (the state does not decay fast enough).
+// piece_phi receives Phi^IIR_TAIL_PIECE, rounded to float32 (2K x 2K, row-major).
+int tail_pieces(const SectionF32* secs, int K, int max_pieces, std::vector<float>& piece_phi) {
+    const int D = 2 * K;
+    std::vector<double> phi(static_cast<size_t>(D) * D, 0.0), newrow(static_cast<size_t>(D));
+    std::vector<double> prev(static_cast<size_t>(D), 0.0);
+    for (int s = 0; s < K; ++s) {
+        std::fill(newrow.begin(), newrow.end(), 0.0);
+        newrow[2 * s + 1] += secs[s].a1;
+        newrow[2 * s] += secs[s].a2;
+        if (s > 0) {
+            for (int j = 0; j < D; ++j) newrow[j] += prev[j];  // y_{s-1}[n] itself (b0 = 1)
+            newrow[2 * (s - 1) + 1] += secs[s].b1;
+            newrow[2 * (s - 1)] += secs[s].b2;
+        }
+        phi[static_cast<size_t>(2 * s) * D + 2 * s + 1] = 1.0;  // y_s[n-1] becomes y_s[n-2]
+        for (int j = 0; j < D; ++j) phi[static_cast<size_t>(2 * s + 1) * D + j] = newrow[j];
+        prev = newrow;
+    }
+    auto mul = [D](const std::vector<double>& a, const std::vector<double>& b) {
+        std::vector<double> r(static_cast<size_t>(D) * D, 0.0);
+        for (int i = 0; i < D; ++i)
+            for (int k = 0; k < D; ++k) {
+                const double aik = a[static_cast<size_t>(i) * D + k];
+                if (aik == 0.0) continue;
+                for (int j = 0; j < D; ++j) r[static_cast<size_t>(i) * D + j] += aik * b[static_cast<size_t>(k) * D + j];
+            }
+        return r;
+    };
+    std::vector<double> m = phi;
+    for (int e = 1; e < IIR_TAIL_PIECE; e *= 2) m = mul(m, m);  // Phi^IIR_TAIL_PIECE
+    piece_phi.assign(m.begin(), m.end());
+    std::vector<double> mp = m;
+    for (int P = 1; P <= max_pieces; ++P) {
+        double norm = 0.0;
+        for (int i = 0; i < D; ++i) {
+            double row = 0.0;
+            for (int j = 0; j < D; ++j) row += std::fabs(mp[static_cast<size_t>(i) * D + j]);
+            norm = std::max(norm, row);
+        }
+        if (!std::isfinite(norm)) return 0;
+        if (norm <= 1e-10) return P;
+        mp = mul(mp, m);
+    }
+    return 0;
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda needed).
@@ -388,6 +458,14 @@ struct iir_plan {
     size_t carry_bytes = 0;
     HostStaging* host = nullptr;      // iir_plan_execute_host: device buffers, streams, events
     unsigned long long* h_err = nullptr;  // host-mapped copy of the device error word (IirLaunchState::host_error)
+    int pieces = 0;                // tail-aggregate pieces of `entry` (0: per-section lookback)
+    // Single-section plans on the persistent two-pass schedule also keep a one-block-per-chunk
+    // kernel for signals of at most small_max_n samples, where the persistent grid's fill and
+    // drain dominate (its own lane tables; tail-aggregate schedule when the filter allows).
+    const KernelEntry* small = nullptr;
+    float4* d_tables_small = nullptr;
+    int small_pieces = 0;
+    size_t small_max_n = 0;
 };
 
 namespace {
@@ -414,9 +492,21 @@ int resolve_auto(int kernel, int n_sections) {
     return n_sections >= 7 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
 }
 
-// samples per block (= per lookback unit)
-size_t chunk_samples(const iir_plan* p) {
-    return p->kind == IIR_KIND_PLR ? static_cast<size_t>(p->B) * p->N : static_cast<size_t>(p->entry->rows) * p->N;
+// samples per block (= per lookback unit) of the plan's large-signal kernel, or of kernel e
+size_t chunk_samples(const iir_plan* p, const KernelEntry* e = nullptr) {
+    if (p->kind == IIR_KIND_PLR) return static_cast<size_t>(p->B) * p->N;
+    return static_cast<size_t>((e ? e : p->entry)->rows) * p->N;
+}
+
+// Largest signal (samples) a single-section plan filters with its one-block-per-chunk kernel
+// instead of the persistent two-pass one (IIR_GB300_SMALL_N; read when a plan is created).
+// Measured on GB300 (butter(2, 0.1), 32x64): PH's one-block-per-chunk kernel on the tail-aggregate
+// schedule is ahead at every size (2^28: 832 against 764 GS/s); for STCR and DTCR it is ahead up to
+// 2^23 samples, the persistent one from 2^24 (DTCR_UNROLL 475 against 446 GS/s there).
+size_t small_signal_limit(int kind, bool tail) {
+    const char* v = std::getenv("IIR_GB300_SMALL_N");
+    if (v) return static_cast<size_t>(std::strtoull(v, nullptr, 10));
+    return (kind == IIR_KIND_PH && tail) ? ~size_t(0) : (size_t(1) << 23);
 }
 
 // 64-bit words of carry slots per section (chunk slots, then one slot per group of chunks)
@@ -487,7 +577,11 @@ int plan_common_alloc(iir_plan* p, size_t max_n) {
     if (st) return st;
     st = attach_host_error(p);
     if (st) return st;
-    const size_t chunk = chunk_samples(p);
+    size_t chunk = chunk_samples(p);
+    if (p->small) {
+        if (blocks_per_sm(*p->small, p->device) <= 0) return IIR_ERR_UNSUPPORTED;
+        chunk = std::min(chunk, chunk_samples(p, p->small));
+    }
     return alloc_carry(p, (std::max<size_t>(max_n, 1) + chunk - 1) / chunk, nullptr);
 }
 
@@ -505,6 +599,7 @@ void plan_free(iir_plan* p) {
     if (p->h_err) cudaFreeHost(p->h_err);
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
+    if (p->d_tables_small) cudaFree(p->d_tables_small);
     if (p->d_fac) cudaFree(p->d_fac);
     delete p;
 }
@@ -556,8 +651,14 @@ int plan_create_plr(iir_plan** out, const double* b, const double* a, int order,
     }
     const int chunk = Bd * Xd;
     const int k = order;
+    // The kernel's in-chunk recurrence runs on the float32-rounded taps, so the factor arrays and
+    // the chunk transition are computed (in FP64) for that same polynomial; built from the
+    // unrounded taps they would describe a different filter, which the ill-conditioned direct
+    // form of order >= 8 turns into errors far above its own rounding.
+    std::vector<double> a32(static_cast<size_t>(order));
+    for (int j = 0; j < order; ++j) a32[j] = static_cast<double>(static_cast<float>(a[j]));
     std::vector<double> fac;
-    plr_factors_f64(a, order, chunk, fac);
+    plr_factors_f64(a32.data(), order, chunk, fac);
     // Phi and its powers (FP64), rounded once
     std::vector<double> phi(static_cast<size_t>(k) * k), P(static_cast<size_t>(k) * k, 0.0), Pg, phig;
     for (int i = 0; i < k; ++i)
@@ -695,7 +796,29 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     int B = block_size, N = n_blocks;
     default_geometry(kernel, n_sections, B, N);
     const KernelEntry* e = nullptr;
+    // The tail-aggregate kernel (iir_tail.cuh) when the cascade's state decays within half a
+    // chunk, in pieces of IIR_TAIL_PIECE samples, one per warp of the block; else nullptr.
+    auto pick_tail = [&](int& pc, std::vector<float>& phi) -> const KernelEntry* {
+        if (tail_max_pieces() <= 0) return nullptr;
+        const KernelEntry* t = find_entry(kernel, B, N, 0, 0, 1);
+        if (!t) return nullptr;
+        const int cap = std::min({tail_max_pieces(), t->threads / 32, IIR_TAIL_MAX_PIECES,
+                                  t->rows * N / (2 * IIR_TAIL_PIECE)});
+        pc = cap > 0 ? tail_pieces(secs.data(), n_sections, cap, phi) : 0;
+        return pc > 0 ? t : nullptr;
+    };
+    int pieces = 0, small_pieces = 0;
+    std::vector<float> phi, small_phi;
+    const KernelEntry* small = nullptr;
     if (n_sections == 1 && pipeline_enabled()) e = find_entry(kernel, B, N, 0, 1);
+    if (e) {
+        // single section on the persistent schedule: a one-block-per-chunk kernel for small signals
+        small = pick_tail(small_pieces, small_phi);
+        if (!small) small = find_entry(kernel, B, N, 0, 0);
+    } else if (n_sections > 1) {
+        // cascades whose state decays within a chunk: one lookback per chunk
+        e = pick_tail(pieces, phi);
+    }
     if (!e) e = find_entry(kernel, B, N, 0, 0);
     if (!e) return IIR_ERR_UNSUPPORTED;
     iir_plan* p = new iir_plan();
@@ -704,20 +827,44 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     p->N = N;
     p->n_sections = n_sections;
     p->entry = e;
+    p->pieces = pieces;
+    p->small = small;
+    p->small_pieces = small_pieces;
+    p->small_max_n = small ? small_signal_limit(kernel, small_pieces > 0) : 0;
     IirParams& q = p->params;
     std::memset(&q, 0, sizeof(q));
-    std::vector<float4> tabs(static_cast<size_t>(n_sections) * IIR_TAB_STRIDE);
-    for (int s = 0; s < n_sections; ++s) {
-        st = precompute_section(secs[s], kernel, e->rows, N, q.sec[s], tabs.data() + static_cast<size_t>(s) * IIR_TAB_STRIDE);
-        if (st) {
-            delete p;
-            return st;
+    // lane tables of every section for kernel k (rows per chunk), then (tail schedule) the
+    // cascade's piece transition
+    auto build_tables = [&](const KernelEntry* k, const std::vector<float>& ph, std::vector<float4>& tabs) {
+        const size_t phi_f4 = (ph.size() + 3) / 4;
+        tabs.assign(static_cast<size_t>(n_sections) * IIR_TAB_STRIDE + phi_f4, make_float4(0, 0, 0, 0));
+        for (int s = 0; s < n_sections; ++s) {
+            IirSection sec;
+            const int r = precompute_section(secs[s], kernel, k->rows, N, sec,
+                                             tabs.data() + static_cast<size_t>(s) * IIR_TAB_STRIDE);
+            if (r) return r;
+            if (k == e) q.sec[s] = sec;  // per-section scalars (the same for both kernels)
         }
+        if (!ph.empty())
+            std::memcpy(tabs.data() + static_cast<size_t>(n_sections) * IIR_TAB_STRIDE, ph.data(),
+                        ph.size() * sizeof(float));
+        return static_cast<int>(IIR_OK);
+    };
+    std::vector<float4> tabs, tabs_small;
+    st = build_tables(e, phi, tabs);
+    if (!st && small) st = build_tables(small, small_phi, tabs_small);
+    if (st) {
+        delete p;
+        return st;
     }
     st = plan_common_alloc(p, max_n);
     if (!st) st = cuda_status(cudaMalloc(&p->d_tables, tabs.size() * sizeof(float4)));
     if (!st)
         st = cuda_status(cudaMemcpy(p->d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    if (!st && small) st = cuda_status(cudaMalloc(&p->d_tables_small, tabs_small.size() * sizeof(float4)));
+    if (!st && small)
+        st = cuda_status(cudaMemcpy(p->d_tables_small, tabs_small.data(), tabs_small.size() * sizeof(float4),
+                                    cudaMemcpyHostToDevice));
     if (st) {
         plan_free(p);
         return st;
@@ -726,6 +873,7 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     q.tables = p->d_tables;
     q.n_sections = n_sections;
     q.gain = static_cast<float>(gain);
+    q.tail_pieces = pieces;
     *out = p;
     return IIR_OK;
 }
@@ -749,7 +897,11 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
         p->withhold = -1;
         return st;
     }
-    const size_t chunk = chunk_samples(p);
+    // the kernel for this signal: a single-section plan's small-signal kernel up to its limit
+    // (a piece that starts from a carried state always takes the persistent schedule)
+    const bool use_small = p->small && !zi && n <= p->small_max_n;
+    const KernelEntry* ent = use_small ? p->small : p->entry;
+    const size_t chunk = chunk_samples(p, ent);
     const size_t nchunks = (n + chunk - 1) / chunk;
     if (nchunks > 0xffffffffull) return IIR_ERR_TOO_LARGE;
     if (nchunks > p->carry_cap) {
@@ -790,24 +942,25 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
         q.nchunks = static_cast<unsigned int>(nchunks);
         q.carry_cap = static_cast<unsigned int>(p->carry_cap);
         q.carry_stride = carry_words_per_section(p, p->carry_cap);
-        const int npr = p->entry->N, rows = p->entry->rows;
-        const bool planes = p->entry->planes != 0;
+        const int npr = ent->N, rows = ent->rows;
+        const bool planes = ent->planes != 0;
         q.use_tma = (aligned && encode_chunk_map(&q.tmap_x, x, static_cast<long long>(n), npr, rows, planes) &&
                      encode_chunk_map(&q.tmap_y, y, static_cast<long long>(n), npr, rows, planes) &&
-                     (!p->entry->pipeline || encode_hist_map(&q.tmap_h, x, static_cast<long long>(n))))
+                     (!ent->pipeline || encode_hist_map(&q.tmap_h, x, static_cast<long long>(n))))
                         ? 1
                         : 0;
         q.timeout_ns = p->timeout_ns;
         q.withhold_chunk = p->withhold;
-        q.zi = p->entry->pipeline ? zi : nullptr;
+        q.zi = ent->pipeline ? zi : nullptr;
+        q.tables = use_small ? p->d_tables_small : p->d_tables;
+        q.tail_pieces = use_small ? p->small_pieces : p->pieces;
         void* args[] = {&q};
-        if (p->entry->pipeline) {
+        if (ent->pipeline) {
             // persistent: at most every resident block, all co-resident (cooperative launch)
             const int pgrid = static_cast<int>(std::min<size_t>(nchunks, static_cast<size_t>(p->grid_max)));
-            err = cudaLaunchCooperativeKernel(p->entry->fn, dim3(pgrid), dim3(p->entry->threads), args,
-                                              p->entry->smem, stream);
+            err = cudaLaunchCooperativeKernel(ent->fn, dim3(pgrid), dim3(ent->threads), args, ent->smem, stream);
         } else {
-            err = cudaLaunchKernel(p->entry->fn, dim3(grid), dim3(p->entry->threads), args, p->entry->smem, stream);
+            err = cudaLaunchKernel(ent->fn, dim3(grid), dim3(ent->threads), args, ent->smem, stream);
         }
     }
     p->withhold = -1;  // one launch only

@@ -16,12 +16,16 @@ struct SectionF32 {
 };
 
 // Registered kernel for (realization, B, N, order, schedule); nullptr if none.
-const iirgb::KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline = 0);
+const iirgb::KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline = 0, int tail = 0);
 // Resident blocks per SM for a registered kernel; also sets its dynamic shared memory limit.
 int blocks_per_sm(const iirgb::KernelEntry& e, int device);
 // scipy SOS rows -> b0 = a0 = 1 sections (FP64 division, float32 result) and the gain.
 int normalise_sos(const float* sos, int n_sections, std::vector<SectionF32>& out, double& gain);
 int normalise_sos(const float* sos, int n_sections, SectionF32* out, double& gain);  // out[n_sections]
+// Tail-aggregate schedule: the least number of IIR_TAIL_PIECE-sample pieces (<= max_pieces) over
+// which the cascade's state decays below 1e-10 (0 if none), and the cascade's transition over one
+// piece (2K x 2K, row-major, float32) in piece_phi.
+int tail_pieces(const SectionF32* secs, int K, int max_pieces, std::vector<float>& piece_phi);
 // One section's kernel coefficients and its IIR_TAB_STRIDE lane-table entries.
 int precompute_section(const SectionF32& s, int kind, int rows, int N, IirSection& q, float4* tab);
 // 2D tensor map over a float32 signal viewed as 128-byte lines, box = lines_per_block lines.

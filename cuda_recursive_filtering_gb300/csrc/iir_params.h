@@ -22,6 +22,7 @@
 //   [TAB_QG + l]   = Q^(32 l)  (group transition powers), l <= 32
 //   [TAB_HALF]     = A^(N/2)   (half-row transition)
 //   [TAB_LBD].x    = truncated lookback depth of the chunk transition (0: two-level lookback)
+//   [TAB_TAIL + l] = (A^16)^(l+1), l < 32 (tail-aggregate schedule: lanes of 16 samples)
 #define IIR_GROUP 32
 #define IIR_TAB_CPOW 0
 #define IIR_TAB_GPOW 256
@@ -29,7 +30,14 @@
 #define IIR_TAB_QG 321
 #define IIR_TAB_HALF 354
 #define IIR_TAB_LBD 355  // .x: truncated lookback depth m (||Q^m|| <= 1e-10, m <= 4), 0 = full lookback
-#define IIR_TAB_STRIDE 356
+#define IIR_TAB_TAIL 356
+#define IIR_TAB_STRIDE 388
+// Tail-aggregate schedule: a chunk's zero-state aggregate is computed from its last
+// tail_pieces x IIR_TAIL_PIECE samples (IirParams::tail_pieces; 0 = per-section lookback), one
+// piece per warp. The cascade's state transition over one piece, Phi^IIR_TAIL_PIECE
+// (2K x 2K floats, row-major), follows the sections' lane tables.
+#define IIR_TAIL_PIECE 512
+#define IIR_TAIL_MAX_PIECES 8
 
 // Device-side per-plan launch state. `ticket` packs the launch epoch (the reference's
 // `launch` index: part_flag = 2*launch+1, full_flag = 2*launch+2; ph_kernels.cuh:16-24) in its
@@ -83,7 +91,7 @@ struct IirParams {
     int n_sections;
     int use_tma;                      // tensor maps valid (x, y 16-byte aligned) -> TMA staging
     float gain;
-    int pad0;
+    int tail_pieces;                  // tail-aggregate kernels: pieces of IIR_TAIL_PIECE samples in the tail
     unsigned long long* prof;         // per-block phase timestamps (IIR_PROFILE builds only)
     IirSection sec[IIR_MAX_SECTIONS];
 };
@@ -115,23 +123,24 @@ struct IirPlrParams {
 // with its own filter and optional state in / state out.
 // State layout (zi / zf, 2 + 2 * n_sections floats): x[-2], x[-1] (raw input), then per
 // section its output history y[-2], y[-1].
-// Compact lane tables per section (rows = IIR_BATCH_ROWS):
-#define IIR_BATCH_ROWS 128
-#ifndef IIR_BATCH_N
-#define IIR_BATCH_N 64  // chunks of 8192 samples (128 rows x 64); 64-sample rows measured 18% faster than 32
-#endif
-#define IIR_BT_CPOW 0      // C^(r+1), r < IIR_BATCH_ROWS
+// Compact lane tables per section, for one chunk shape (ROWS rows of N samples, ROWS <= 128):
+#define IIR_BATCH_MAX_ROWS 128
+#define IIR_BT_CPOW 0      // C^(r+1), r < ROWS          (C = A^N)
 #define IIR_BT_GPOW 128    // C^(t+1), t < 32
-#define IIR_BT_QC 160      // Q^l, l <= 32
+#define IIR_BT_QC 160      // Q^l, l <= 32               (Q = C^ROWS, the chunk transition)
 #define IIR_BT_QG 193      // Q^(32 l), l <= 32
 #define IIR_BT_LBD 226     // .x: truncated lookback depth (0: two-level lookback)
-#define IIR_BT_STRIDE 228
+#define IIR_BT_TAIL 228    // (A^16)^(l+1), l < 32        (tail-aggregate schedule)
+#define IIR_BT_STRIDE 260
+// Phi^IIR_TAIL_PIECE of a filter's cascade (2K x 2K floats, row-major), one block of this many
+// floats per filter
+#define IIR_BT_PHI_FLOATS (4 * IIR_MAX_SECTIONS * IIR_MAX_SECTIONS)
 
 struct IirBatchFilter {
     float gain;
     int n_sections;
     int sec0;               // index of its first section in the section / table arrays
-    int pad;
+    int tail;               // tail-aggregate pieces for the batch's chunk shape (0: per-section lookback)
 };
 
 struct IirBatchSegment {
@@ -151,7 +160,8 @@ struct IirBatchParams {
     const unsigned int* chunk_start;  // [nsegs + 1], chunk_start[i] = segs[i].chunk0
     const IirBatchFilter* filters;
     const IirSection* secs;
-    const float4* tables;             // [sections][IIR_BT_STRIDE]
+    const float4* tables;             // [sections][IIR_BT_STRIDE], for the launch's chunk shape
+    const float* phi;                 // [filters][IIR_BT_PHI_FLOATS]
     unsigned long long* carry;        // per section level: [carry_cap][4] chunk slots, then [gcap][4] group slots
     IirLaunchState* state;
     unsigned long long carry_stride;  // words per section level

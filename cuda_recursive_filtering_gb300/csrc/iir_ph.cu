@@ -18,10 +18,22 @@ __global__ void __launch_bounds__(32 + ROWS, BlockGeom<ROWS, N>::min_blocks(32 +
     PhBlock<B, N, ROWS>::run(p, smem);
 }
 
+// Cascade kernel on the tail-aggregate schedule (iir_tail.cuh): one lookback per chunk.
+template <int B, int N, int ROWS>
+__global__ void __launch_bounds__(32 + ROWS, BlockGeom<ROWS, N>::min_blocks(32 + ROWS))
+    iir_ph_tail_kernel(const __grid_constant__ IirParams p) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    PhBlock<B, N, ROWS, true>::run(p, smem);
+}
+
 template <int B, int N, int ROWS>
 static void add_ph(std::vector<KernelEntry>& reg) {
     reg.push_back(KernelEntry{IIR_KIND_PH, B, N, (const void*)iir_ph_kernel<B, N, ROWS>, 32 + ROWS,
                               BlockGeom<ROWS, N>::SMEM_BYTES, 0, ROWS});
+    KernelEntry t{IIR_KIND_PH, B, N, (const void*)iir_ph_tail_kernel<B, N, ROWS>, 32 + ROWS,
+                  BlockGeom<ROWS, N>::SMEM_BYTES, 0, ROWS};
+    t.tail = 1;
+    reg.push_back(t);
 }
 
 #ifndef IIR_TWO_STAGES

@@ -18,13 +18,17 @@
 // than in registers. A thread needs ~30 registers, so up to a dozen blocks share an SM and
 // their loads and lookback waits overlap each other's filtering (the lookback latency is
 // set by the slowest predecessor's load, so concurrency, not a faster poll, hides it).
+// With TAIL (iir_tail.cuh), the control warp resolves every section's incoming state once per
+// chunk from the predecessor's tail aggregate, and steps 3 and 4 read it from shared memory: the
+// row warps meet at one barrier per section (among themselves) instead of two around a lookback.
 #pragma once
 #include "iir_device.cuh"
+#include "iir_tail.cuh"
 #include "iir_twopass.cuh"
 
 namespace iirgb {
 
-template <int B_, int N_, int ROWS_>
+template <int B_, int N_, int ROWS_, bool TAIL = false>
 struct PhBlock {
     static constexpr int B = B_, N = N_, ROWS = ROWS_;
     static constexpr int NW = ROWS / 32;           // row warps
@@ -54,7 +58,7 @@ struct PhBlock {
                                        float pa2, float d2, float d1, float& xh2, float& xh1, float& s0,
                                        float& s1) {
         float y1 = 0.f, y2 = 0.f;
-#pragma unroll 4
+#pragma unroll
         for (int j = 0; j < N / 4; ++j) {
             float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
             const float4 q = *ptr;
@@ -85,7 +89,7 @@ struct PhBlock {
 
     // Final correction pass (last section): row += response to the incoming state.
     __device__ static void correct_pass(float* buf, int r, float a1, float a2, float d2, float d1) {
-#pragma unroll 4
+#pragma unroll
         for (int j = 0; j < N / 4; ++j) {
             float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
             const float4 q = *ptr;
@@ -105,6 +109,10 @@ struct PhBlock {
     __device__ static bool filter_block(const IirParams& p, float* buf, BlockAux* aux, uint32_t c, uint32_t epoch,
                                         int warp, int lane) {
         const bool row_warp = warp > 0;
+        if constexpr (TAIL) {
+            bool ok = true;
+            if (!tail_begin<N, ROWS, true>(p, buf, aux, c, epoch, warp, ok)) return ok;  // control warp
+        }
         const int w = warp - 1;
         const int r = w * 32 + lane;  // row index (row warps)
         float xh2 = 0.f, xh1 = 0.f;   // input history of this row
@@ -145,13 +153,16 @@ struct PhBlock {
                 // scan of row tails (zero block state)
                 warp_scan2<32, 1>(s0, s1, q.M, lane);
                 if (lane == 31) {
-                    aux->wtot[w][0][0] = s0;
-                    aux->wtot[w][0][1] = s1;
+                    aux->wtot[w][TAIL ? (sec & 1) : 0][0] = s0;
+                    aux->wtot[w][TAIL ? (sec & 1) : 0][1] = s1;
                 }
             }
-            __syncthreads();  // (A)
+            // (A); the tail schedule alternates the warp totals' buffers, so one barrier per section
+            // separates a section's reads from the next section's writes
+            if (!TAIL || sec == 0) __syncthreads();
+            else named_barrier_rows(NW);
             if (row_warp) {
-                warp_incoming(aux, w, 0, Gw, in0, in1);  // zero-state tail before this warp
+                warp_incoming(aux, w, TAIL ? (sec & 1) : 0, Gw, in0, in1);  // zero-state tail before this warp
                 if (w > 0) {
                     float e0, e1;
                     mv2(tab[IIR_TAB_GPOW + lane], in0, in1, e0, e1);
@@ -159,11 +170,13 @@ struct PhBlock {
                     s1 += e1;
                 }
             }
-            if (!row_warp) control_section<NW, 1>(p, aux, sec, c, epoch, tab, Gw);
-            __syncthreads();  // (B)
+            if (!TAIL) {
+                if (!row_warp) control_section<NW, 1>(p, aux, sec, c, epoch, tab, Gw);
+                __syncthreads();  // (B)
+            }
             if (aux->bail) return false;
             if (row_warp) {
-                const float X0 = aux->X[0], X1 = aux->X[1];
+                const float X0 = TAIL ? aux->Xs[sec][0] : aux->X[0], X1 = TAIL ? aux->Xs[sec][1] : aux->X[1];
                 // true tails and the true incoming state of this row
                 float P0, P1;
                 mv2(tab[IIR_TAB_CPOW + r], X0, X1, P0, P1);

@@ -46,6 +46,8 @@ struct PipeAux {
     float partv[8][2];
     float xv[8][2];
     float wtot[16][2][2];
+    float xch[2][16][2];    // cyclic-reduction tiles over several warps: per-level row hand-off
+    float xscan[16][2][2];  // and the warps' top-level scan totals
     unsigned int epoch;
     int bail;      // lookback gave up: no more stores
     int abandon;   // an mbarrier wait ran out: skip every remaining wait

@@ -29,6 +29,7 @@ struct KernelEntry {
     int rows;       // rows per block (tiles x B) for the row-major realizations
     int pipeline = 0;  // 1: single-section persistent pipeline, launched cooperatively
     int planes = 1;    // chunk buffer layout: 1 = planes of 32-sample columns, 0 = lines (swz)
+    int tail = 0;      // 1: cascade kernel on the tail-aggregate schedule (iir_tail.cuh)
 };
 
 void register_ph(std::vector<KernelEntry>& reg);

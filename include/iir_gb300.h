@@ -183,9 +183,10 @@ typedef struct iir_batch iir_batch;
  * (sum of n_sections[f] rows of 6), n_sections[f] in 1..8. Capacities grow on demand. */
 int iir_batch_create(iir_batch** batch, const float* sos, const int* n_sections, int n_filters,
                      size_t max_segments, size_t max_chunks);
-/* Filters every segment in one launch on `stream` (PH solve, chunks of 8192 samples, the
- * decoupled lookback restricted to each segment). Stream-ordered; launches of one batch
- * plan must be ordered on one stream at a time. */
+/* Filters every segment in one launch on `stream`: a persistent grid draws the segments' chunks
+ * from one work queue (PH solve; the decoupled lookback restricted to each segment; filters whose
+ * state decays within half a chunk publish one aggregate per chunk from its tail, the others one
+ * per section). Stream-ordered; launches of one batch plan must be ordered on one stream. */
 int iir_batch_execute(iir_batch* batch, const iir_segment* segs, int n_segs, void* stream);
 int iir_batch_check(iir_batch* batch, void* stream);
 /* A fixed segment table uploaded once (synchronously) for repeated launches: each
@@ -201,6 +202,16 @@ int iir_batch_set_timeout_ns(iir_batch* batch, long long timeout_ns);
 int iir_batch_debug_withhold(iir_batch* batch, long long chunk);
 /* Sections of filter `filter` (the state length is 2 + 2 * sections). */
 int iir_batch_filter_sections(const iir_batch* batch, int filter);
+/* Chunk shape of the batch's later launches: rows x samples_per_row, one of 128 x 64 (the
+ * default), 128 x 32, 128 x 16 and 64 x 16 (chunks of 8192 down to 1024 samples; a segment
+ * occupies whole chunks, so short segments want small ones). IIR_ERR_UNSUPPORTED for any other.
+ * Handles bound earlier keep their shape. The tuner in autotune.py chooses it per workload. */
+int iir_batch_set_shape(iir_batch* batch, int rows, int samples_per_row);
+/* The current chunk shape, its kernel's threads per block, registers per thread and shared memory
+ * per block, and the resident blocks per SM (the persistent grid is that times the SM count, or
+ * the number of chunks if fewer). Any pointer may be NULL. */
+int iir_batch_get_shape(const iir_batch* batch, int* rows, int* samples_per_row, int* threads,
+                        int* regs_per_thread, int* smem_bytes, int* blocks_per_sm);
 int iir_batch_destroy(iir_batch* batch);
 
 /* ---- helpers ------------------------------------------------------------------------- */

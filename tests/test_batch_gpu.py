@@ -182,3 +182,112 @@ def test_bound_batch_replays_in_a_cuda_graph(cuda_device):
     batch.check()
     assert torch.allclose(y_graph, y_direct, rtol=0, atol=1e-6 * float(y_direct.abs().max()))
     bound.close()
+
+
+def _mixed_filters():
+    """Filters on both schedules: most decay within half a chunk (tail aggregate); butter(2, 0.003)
+    and butter(16, 0.05) do not at any shape (per-section lookback)."""
+    from scipy import signal
+    return _filters() + [(2, signal.butter(2, 0.003, output="sos")), (16, signal.butter(16, 0.05, output="sos"))]
+
+
+@pytest.mark.parametrize("shape", [(128, 64), (128, 32), (128, 16), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_every_chunk_shape(shape, cuda_device):
+    """Every compiled chunk shape of the persistent batch kernel, channels of many lengths around
+    the chunk size with filters on both schedules, two launches in a row (new epoch, same slots)."""
+    filters = _mixed_filters()
+    batch = Batch([s for _, s in filters])
+    batch.set_shape(*shape)
+    sh = batch.shape()
+    assert (sh["rows"], sh["samples_per_row"]) == shape and sh["blocks_per_sm"] > 0
+    chunk = sh["chunk"]
+    rng = np.random.default_rng(shape[1])
+    lengths = [1, 5, chunk - 1, chunk, chunk + 1, 3 * chunk + 17, 20 * chunk + 5]
+    lengths += [int(v) for v in rng.integers(1, 30 * chunk, 24)]
+    chans = []
+    for i, n in enumerate(lengths):
+        f = i % len(filters)
+        x = rng.uniform(-1, 1, n).astype(np.float32)
+        xt = torch.from_numpy(x).cuda()
+        chans.append((x, xt, torch.empty_like(xt), f))
+    for launch in range(2):
+        for _, _, yt, _ in chans:
+            yt.fill_(float("nan"))
+        batch([(xt, yt, f) for _, xt, yt, f in chans])
+        batch.check()
+        for i, (x, _, yt, f) in enumerate(chans):
+            _check(yt.cpu().numpy(), x, filters[f][1], filters[f][0], (shape, launch, i, x.size, f))
+
+
+@pytest.mark.parametrize("shape", [(128, 64), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_streamed_state_both_schedules(shape, cuda_device):
+    """A stream in random pieces with its state carried on the device, for a filter on the tail
+    schedule and one on the per-section lookback, at the largest and smallest chunk shapes."""
+    filters = _mixed_filters()
+    batch = Batch([s for _, s in filters])
+    batch.set_shape(*shape)
+    rng = np.random.default_rng(7)
+    for f in (2, len(filters) - 2):
+        n = 120_000
+        x = rng.uniform(-1, 1, n).astype(np.float32)
+        xt = torch.from_numpy(x).cuda()
+        yt = torch.empty_like(xt)
+        st = [torch.zeros(batch.state_size(f), device="cuda") for _ in range(2)]
+        pos, turn = 0, 0
+        while pos < n:
+            m = min(int(rng.integers(1, 30000)), n - pos)
+            batch([(xt[pos:pos + m], yt[pos:pos + m], f, st[turn], st[turn ^ 1])])
+            pos += m
+            turn ^= 1
+        batch.check()
+        _check(yt.cpu().numpy(), x, filters[f][1], filters[f][0], ("stream", shape, f))
+
+
+def test_tail_and_per_section_schedules_agree(monkeypatch, cuda_device):
+    """The same channels with the tail-aggregate schedule and with the per-section lookback
+    everywhere (IIR_GB300_TAIL=0, read when a shape is prepared): both meet the gate and agree to
+    1e-5 of the signal's peak."""
+    filters = _mixed_filters()
+    rng = np.random.default_rng(8)
+    lengths = [int(v) for v in rng.integers(1, 200_000, 30)]
+    xs = [rng.uniform(-1, 1, n).astype(np.float32) for n in lengths]
+    outs = []
+    for tail in (True, False):
+        if not tail:
+            monkeypatch.setenv("IIR_GB300_TAIL", "0")
+        batch = Batch([s for _, s in filters])
+        ys = [torch.empty(x.size, device="cuda") for x in xs]
+        batch([(torch.from_numpy(x).cuda(), y, i % len(filters)) for i, (x, y) in enumerate(zip(xs, ys))])
+        batch.check()
+        outs.append([y.cpu().numpy() for y in ys])
+    for i, x in enumerate(xs):
+        order, sos = filters[i % len(filters)]
+        _, ref = oracle.reference_golden(sos, x)
+        scale = float(np.max(np.abs(ref))) or 1.0
+        assert np.max(np.abs(outs[0][i] - outs[1][i])) <= 1e-5 * scale, i
+        _check(outs[0][i], x, sos, order, ("tail", i))
+
+
+def test_tune_batch_picks_a_shape_and_filters_correctly(cuda_device):
+    """The batching tuner times every compiled shape in the order the occupancy model proposes
+    and leaves the fastest set; the batch still filters correctly with it."""
+    from cuda_recursive_filtering_gb300 import autotune
+    filters = _mixed_filters()
+    batch = Batch([s for _, s in filters])
+    rng = np.random.default_rng(9)
+    lengths = rng.integers(500, 3000, 2000)
+    off = np.concatenate([[0], np.cumsum(lengths)])
+    x = torch.from_numpy(rng.uniform(-1, 1, int(off[-1])).astype(np.float32)).cuda()
+    y = torch.empty_like(x)
+    flt = (np.arange(lengths.size) % len(filters)).astype(np.int32)
+    res = autotune.tune_batch(batch, x, y, off, flt, reps=2)
+    assert len(res["table"]) == 4 and all(t["gsps"] > 0 for t in res["table"])
+    assert [batch.shape()["rows"], batch.shape()["samples_per_row"]] == res["shape"]
+    # short segments: the model ranks the small chunks first (less padding)
+    assert res["model_order"][0][0] * res["model_order"][0][1] <= 2048
+    batch.packed(x, y, off, flt)
+    batch.check()
+    yh = y.cpu().numpy()
+    for i in rng.choice(lengths.size, 12, replace=False):
+        f = int(flt[i])
+        _check(yh[off[i]:off[i + 1]], x[off[i]:off[i + 1]].cpu().numpy(), filters[f][1], filters[f][0], ("tuned", i))

@@ -21,6 +21,13 @@ from cuda_recursive_filtering_gb300 import Plan
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def _persistent_schedule_at_every_size(monkeypatch):
+    # single-section plans take a one-block-per-chunk kernel up to 2^23 samples by default;
+    # these tests are about the persistent two-pass schedule, so it takes every size here
+    monkeypatch.setenv("IIR_GB300_SMALL_N", "0")
+
 PIPE_KERNELS = ["PH", "STCR", "STCR_UNROLL", "DTCR", "DTCR_UNROLL"]
 PIPE_GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
 

@@ -10,9 +10,10 @@ different filters and sizes check that the shared array carries nothing wrong fr
 to the next (launch-versioned carry slots, rewritten tables).
 Tolerances (the ones the parity tests use): against the FP64 oracle, max|err| <= 1e-4 *
 max|ref| (the reference's gate, src/test_accuracy.cu:178-188) and max|err| / RMS(ref) <= 1e-5
-(2e-5 at order 16). Against iir_sos_filter: cascades run the same PH kernel with the same
-tables, so they agree to 1e-6 * max|ref|; order 2 runs the one-block-per-chunk PH kernel here
-and the two-pass schedule there, so the two agree to the gate.
+(2e-5 at order 16). Against iir_sos_filter: max|noalloc - iir_sos_filter| <= 1e-5 * max|ref|,
+the bound the parity tests put on two schedules of one realization (this entry point runs the
+PH kernel with one lookback per section; iir_sos_filter may pick another schedule of PH for the
+same filter, so the two agree to rounding, not bit for bit).
 """
 import ctypes
 
@@ -65,8 +66,7 @@ def test_noalloc_matches_sos_filter(cuda_device):
         assert e["finite"], (order, n)
         assert e["rel_max"] <= 1e-4, (order, n, e)
         assert e["rel_rms"] <= (2e-5 if order == 16 else 1e-5), (order, n, e)
-        agree = 1e-6 if order > 2 else 1e-4
-        assert np.max(np.abs(a - b)) <= agree * scale, (order, n)
+        assert np.max(np.abs(a - b)) <= 1e-5 * scale, (order, n)
         del x, y_na, y_ref
 
 
