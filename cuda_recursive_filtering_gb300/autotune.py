@@ -122,10 +122,13 @@ def tuned_plan(sos, n: int, **kw) -> Plan:
 # GTX 1070 and RTX 3060 profiles only, and compiling elsewhere silently uses the RTX 3060 one).
 # GB300 profile (sm_103a): 228 KB of shared memory per SM with 1 KB reserved per resident block,
 # 227 KB per block at most, 64 Ki registers, 2048 threads, 64 warps and 32 blocks per SM.
+# chunk_overhead_samples: the fixed cost of one chunk of the batch kernel (draw, segment search,
+# barriers, lookback) in sample-equivalents, fitted on GB300 to one 2^28-sample segment filtered
+# with each shape: a block's time per chunk is about 3.5 us + 0.97 ns per sample of the chunk.
 GB300 = {"name": "GB300 (sm_103a)", "num_sms": 152, "registers_per_sm": 65536, "shared_mem_per_sm": 228 * 1024,
          "reserved_shared_mem_per_tb": 1024, "max_shared_mem_per_tb": 227 * 1024, "max_threads_per_sm": 2048,
          "max_warps_per_sm": 64, "max_tbs_per_sm": 32, "max_threads_per_tb": 1024, "warp_size": 32,
-         "register_alloc_unit": 256}
+         "register_alloc_unit": 256, "chunk_overhead_samples": 3600}
 
 
 def supply_blocks_per_sm(threads: int, regs_per_thread: int, smem_bytes: int, prof: dict = GB300) -> int:
@@ -151,12 +154,12 @@ def demand_blocks_per_sm(chunks: int, prof: dict = GB300) -> int:
 
 
 def rank_batch_shapes(shapes: list[dict], lengths, prof: dict = GB300) -> list[dict]:
-    """Orders candidate chunk shapes for segments of the given lengths. For each shape, the
-    effective residency min(supply, demand) (gpu_specs.hpp:100-104) gives the samples in flight
-    per SM (residency x chunk), and the padding past every segment's end gives the fraction of the
-    launch's work that is useful. The score is useful fraction x in-flight samples, saturating at
-    the in-flight depth the largest shape reaches at full residency: work a chunk does not fill is
-    lost, and a shape that cannot keep enough samples in flight leaves HBM idle."""
+    """Orders candidate chunk shapes for segments of the given lengths, fastest predicted first.
+    A shape's launch keeps `resident` = min(supply, demand) blocks per SM busy (the reference's
+    effective residency, gpu_specs.hpp:100-104); each block takes chunks one after another at
+    (chunk_overhead_samples + chunk) sample-times per chunk, padding past a segment's end
+    included. Predicted time = chunks / (resident x SMs) waves of that; score = the segments'
+    samples / predicted time, normalised to the best shape. `useful` is the unpadded fraction."""
     lengths = np.asarray(lengths, dtype=np.int64)
     total = int(lengths.sum())
     rows = []
@@ -165,11 +168,14 @@ def rank_batch_shapes(shapes: list[dict], lengths, prof: dict = GB300) -> list[d
         chunks = int(np.sum(-(-lengths // chunk)))
         supply = supply_blocks_per_sm(sh["threads"], sh["regs_per_thread"], sh["smem_bytes"], prof)
         resident = min(supply, demand_blocks_per_sm(chunks, prof))
+        slots = max(1, resident * prof["num_sms"])
+        waves = max(1.0, chunks / slots)
         rows.append(dict(sh, chunks=chunks, supply=supply, resident=resident,
-                         useful=total / max(1, chunks * chunk), in_flight=resident * chunk))
-    depth = max(r["supply"] * r["chunk"] for r in rows) or 1
+                         useful=total / max(1, chunks * chunk),
+                         predicted=waves * (prof["chunk_overhead_samples"] + chunk)))
+    best = min(r["predicted"] for r in rows) or 1.0
     for r in rows:
-        r["score"] = r["useful"] * min(1.0, r["in_flight"] / depth)
+        r["score"] = best / r["predicted"]
     return sorted(rows, key=lambda r: -r["score"])
 
 

@@ -44,10 +44,10 @@
 namespace iirgb {
 
 struct BatchAux {
-    unsigned int chunk, epoch, seg;
+    unsigned int chunk, seg;  // the chunk the block drew, and its segment
+    int more;                 // the draw found a chunk of this launch
+    unsigned int epoch;
     int bail;
-    int more;  // the block drew a chunk of this launch
-    int pad[3];
     float wtot[16][2][2];
     float X[2];
     float Xs[IIR_MAX_SECTIONS][2];                           // tail schedule: incoming states
@@ -61,6 +61,9 @@ struct BatchBlock {
     static_assert(ROWS % 32 == 0 && ROWS <= IIR_BATCH_MAX_ROWS, "rows per chunk");
     using Ph = PhBlock<32, N, ROWS>;
     static constexpr size_t SMEM_BYTES = CHUNK * sizeof(float) + sizeof(BatchAux) + 16;
+    // resident blocks per SM the kernel is compiled for (registers), at most what shared memory allows
+    static constexpr int SMEM_BLOCKS = static_cast<int>((228 * 1024) / (SMEM_BYTES + 1024));
+    static constexpr int MIN_BLOCKS = SMEM_BLOCKS < 6 ? SMEM_BLOCKS : 6;
     // tail pieces a chunk of this shape takes: one per warp, at most half of the chunk
     static constexpr int MAX_PIECES_RAW = WARPS < IIR_TAIL_MAX_PIECES ? WARPS : IIR_TAIL_MAX_PIECES;
     static constexpr int MAX_PIECES = MAX_PIECES_RAW < CHUNK / (2 * IIR_TAIL_PIECE) ? MAX_PIECES_RAW
@@ -136,52 +139,40 @@ struct BatchBlock {
             aux->chunk = c;
             aux->seg = lo;
             aux->more = more ? 1 : 0;
-            aux->bail = 0;
         }
     }
 
-    // One chunk (all threads). Returns false when a wait of this launch gave up (uniform).
-    __device__ static bool chunk(const IirBatchParams& p, float* buf, BatchAux* aux, int tid, int warp, int lane) {
-        const uint32_t c = aux->chunk, epoch = aux->epoch;
-        const IirBatchSegment sg = p.segs[aux->seg];
+    // All threads: start copying chunk c of segment `seg` into buf (cp.async, no registers held),
+    // zero past the segment's end. Whole chunks of a 16-byte-aligned segment move as 16-byte
+    // copies, the rest sample by sample. Completion: the caller's cp_async_wait and barrier.
+    __device__ static void stage(const IirBatchParams& p, uint32_t c, uint32_t seg, float* buf, int tid) {
+        const IirBatchSegment& sg = p.segs[seg];
+        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
+        const long long nrem = sg.n - cs;  // > 0
+        const float* src = sg.x + cs;
+        if (nrem >= CHUNK && (reinterpret_cast<uintptr_t>(sg.x) & 15u) == 0) {
+#pragma unroll 4
+            for (int i = tid; i < CHUNK / 4; i += THREADS)
+                cp_async16(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N), src + 4 * i);
+        } else {
+#pragma unroll 4
+            for (int i = tid; i < CHUNK; i += THREADS) {
+                const bool in = i < nrem;
+                cp_async4(buf + swz<N, ROWS, true>(i / N, i % N), in ? src + i : src, in ? 4 : 0);
+            }
+        }
+    }
+
+    // One chunk (all threads), already staged in buf. Returns false when a wait of this launch
+    // gave up (uniform).
+    __device__ static bool chunk(const IirBatchParams& p, float* buf, BatchAux* aux, uint32_t c, uint32_t seg, int tid,
+                                 int warp, int lane) {
+        const uint32_t epoch = aux->epoch;
+        const IirBatchSegment sg = p.segs[seg];
         const IirBatchFilter flt = p.filters[sg.filter];
         const uint32_t lc = c - sg.chunk0;
         const long long cs = static_cast<long long>(lc) * CHUNK;
         const long long nrem = sg.n - cs;  // samples of the segment from this chunk's start (> 0)
-        if (nrem >= CHUNK && (reinterpret_cast<uintptr_t>(sg.x) & 15u) == 0) {
-            // whole chunk, 16-byte aligned: float4 loads, all issued before the stores
-            constexpr int V = CHUNK / 4, PER = (V + THREADS - 1) / THREADS;
-            const float4* src = reinterpret_cast<const float4*>(sg.x + cs);
-            float4 v[PER];
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int i = tid + k * THREADS;
-                if (i < V) v[k] = __ldg(src + i);
-            }
-#pragma unroll
-            for (int k = 0; k < PER; ++k) {
-                const int i = tid + k * THREADS;
-                if (i < V) *reinterpret_cast<float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N)) = v[k];
-            }
-        } else {
-            // unaligned or partial chunk: coalesced scalar loads, a batch of them in flight per
-            // thread before the stores (zero past the segment's end)
-            constexpr int PS = (CHUNK + THREADS - 1) / THREADS, BT = 8;
-            for (int k0 = 0; k0 < PS; k0 += BT) {
-                float t[BT];
-#pragma unroll
-                for (int k = 0; k < BT; ++k) {
-                    const int i = tid + (k0 + k) * THREADS;
-                    t[k] = (i < CHUNK && i < nrem) ? __ldg(sg.x + cs + i) : 0.f;
-                }
-#pragma unroll
-                for (int k = 0; k < BT; ++k) {
-                    const int i = tid + (k0 + k) * THREADS;
-                    if (i < CHUNK) buf[swz<N, ROWS, true>(i / N, i % N)] = t[k];
-                }
-            }
-        }
-        __syncthreads();
 
         const bool row_warp = warp > 0;
         const int K = flt.n_sections;
@@ -349,7 +340,11 @@ struct BatchBlock {
     }
 
     // Persistent block: chunks from the launch's queue until it is empty (or a wait gave up);
-    // the last block to leave re-arms the queue for the next launch with the next epoch.
+    // the last block to leave re-arms the queue for the next launch with the next epoch. A block
+    // starts filtering every chunk it draws at once: a drawn chunk that waited for its block
+    // (to prefetch it, say) would hold up its segment's later chunks, which wait for its carries.
+    // The copy-in latency is hidden by the other resident blocks instead (the kernel is compiled
+    // for several per SM, and its staging holds no registers).
     __device__ static void run(const IirBatchParams& p, unsigned char* smem) {
         float* buf = reinterpret_cast<float*>(smem);
         BatchAux* aux = reinterpret_cast<BatchAux*>(smem + CHUNK * sizeof(float));
@@ -358,9 +353,14 @@ struct BatchBlock {
             aux->epoch = static_cast<uint32_t>(*reinterpret_cast<volatile unsigned long long*>(&p.state->ticket) >> 32);
         while (true) {
             if (warp == 0) draw(p, aux, lane);
-            __syncthreads();
+            __syncthreads();  // also: the previous chunk's store has read the buffer
             if (!aux->more) break;
-            if (!chunk(p, buf, aux, tid, warp, lane)) break;
+            const uint32_t c = aux->chunk, seg = aux->seg;
+            stage(p, c, seg, buf, tid);
+            cp_async_commit();
+            cp_async_wait<0>();
+            __syncthreads();
+            if (!chunk(p, buf, aux, c, seg, tid, warp, lane)) break;
         }
         __syncthreads();
         if (tid == 0) pipe_finish(p.state, aux->epoch);
@@ -368,7 +368,7 @@ struct BatchBlock {
 };
 
 template <int N, int ROWS>
-__global__ void __launch_bounds__(BatchBlock<N, ROWS>::THREADS, 4) iir_batch_kernel(const __grid_constant__ IirBatchParams p) {
+__global__ void __launch_bounds__(BatchBlock<N, ROWS>::THREADS, BatchBlock<N, ROWS>::MIN_BLOCKS) iir_batch_kernel(const __grid_constant__ IirBatchParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     BatchBlock<N, ROWS>::run(p, smem);
 }
@@ -406,10 +406,12 @@ const std::vector<ShapeDef>& shapes() {
     return s;
 }
 
-// Per-shape device data: lane tables of every section and the filters (with each filter's
-// schedule for this shape), built when the shape is first used; the occupancy of its kernel.
+// Per-shape device data: the sections' scalars and lane tables (both depend on the samples per
+// row) and the filters (with each filter's schedule for this shape), built when the shape is
+// first used; the occupancy of its kernel.
 struct ShapeData {
     bool ready = false;
+    IirSection* d_secs = nullptr;
     float4* d_tables = nullptr;
     IirBatchFilter* d_filters = nullptr;
     int blocks_per_sm = 0;
@@ -427,7 +429,6 @@ struct iir_batch {
     std::vector<SectionF32> sec32;
     std::vector<IirBatchFilter> filters;
     std::vector<int> tail_need;  // least number of tail pieces for the filter's state to decay (0: > 8)
-    IirSection* d_secs = nullptr;
     float* d_phi = nullptr;
     std::vector<ShapeData> shape_data;
     int shape = 0;  // index into shapes()
@@ -499,10 +500,10 @@ void batch_free(iir_batch* b) {
     for (int i = 0; i < 2; ++i)
         if (b->stage_done[i]) cudaEventDestroy(b->stage_done[i]);
     for (ShapeData& d : b->shape_data) {
+        if (d.d_secs) cudaFree(d.d_secs);
         if (d.d_tables) cudaFree(d.d_tables);
         if (d.d_filters) cudaFree(d.d_filters);
     }
-    if (b->d_secs) cudaFree(b->d_secs);
     if (b->d_phi) cudaFree(b->d_phi);
     if (b->d_state) cudaFree(b->d_state);
     if (b->d_carry) cudaFree(b->d_carry);
@@ -522,9 +523,10 @@ int shape_prepare(iir_batch* b, int k) {
     if (d.ready) return IIR_OK;
     const ShapeDef& sd = shapes()[static_cast<size_t>(k)];
     std::vector<float4> tabs(b->sec32.size() * IIR_BT_STRIDE, make_float4(0, 0, 0, 0));
+    std::vector<IirSection> secs(b->sec32.size());
     std::vector<float4> full(IIR_TAB_STRIDE);
     for (size_t s = 0; s < b->sec32.size(); ++s) {
-        IirSection q;
+        IirSection& q = secs[s];
         const int st = precompute_section(b->sec32[s], IIR_KIND_PH, sd.rows, sd.n, q, full.data());
         if (st) return st;
         float4* t = tabs.data() + s * IIR_BT_STRIDE;
@@ -543,7 +545,9 @@ int shape_prepare(iir_batch* b, int k) {
         const int need = b->tail_need[f];
         flt[f].tail = (tail_on && need > 0 && need <= sd.max_pieces) ? need : 0;
     }
-    int st = cuda_status(cudaMalloc(&d.d_tables, tabs.size() * sizeof(float4)));
+    int st = cuda_status(cudaMalloc(&d.d_secs, secs.size() * sizeof(IirSection)));
+    if (!st) st = cuda_status(cudaMemcpy(d.d_secs, secs.data(), secs.size() * sizeof(IirSection), cudaMemcpyHostToDevice));
+    if (!st) st = cuda_status(cudaMalloc(&d.d_tables, tabs.size() * sizeof(float4)));
     if (!st) st = cuda_status(cudaMemcpy(d.d_tables, tabs.data(), tabs.size() * sizeof(float4), cudaMemcpyHostToDevice));
     if (!st) st = cuda_status(cudaMalloc(&d.d_filters, flt.size() * sizeof(IirBatchFilter)));
     if (!st)
@@ -571,7 +575,7 @@ IirBatchParams batch_params(const iir_batch* b, int k, const IirBatchSegment* se
     q.segs = segs;
     q.chunk_start = starts;
     q.filters = b->shape_data[static_cast<size_t>(k)].d_filters;
-    q.secs = b->d_secs;
+    q.secs = b->shape_data[static_cast<size_t>(k)].d_secs;
     q.tables = b->shape_data[static_cast<size_t>(k)].d_tables;
     q.phi = b->d_phi;
     q.carry = b->d_carry;
@@ -614,10 +618,7 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
     b->n_filters = n_filters;
     b->filters.resize(static_cast<size_t>(n_filters));
     b->tail_need.assign(static_cast<size_t>(n_filters), 0);
-    std::vector<IirSection> secs;
     std::vector<float> phi(static_cast<size_t>(n_filters) * IIR_BT_PHI_FLOATS, 0.f);
-    std::vector<float4> full(IIR_TAB_STRIDE);
-    const ShapeDef& sd0 = shapes()[0];
     int max_sec = 1;
     size_t off = 0;
     for (int f = 0; f < n_filters; ++f) {
@@ -633,17 +634,10 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
             delete b;
             return st;
         }
-        b->filters[static_cast<size_t>(f)] = IirBatchFilter{static_cast<float>(gain), ns, static_cast<int>(secs.size()), 0};
-        for (int k = 0; k < ns; ++k) {
-            IirSection q;
-            st = precompute_section(s32[k], IIR_KIND_PH, sd0.rows, sd0.n, q, full.data());
-            if (st) {
-                delete b;
-                return st;
-            }
-            secs.push_back(q);
-            b->sec32.push_back(s32[k]);
-        }
+        // the sections' scalars and lane tables depend on the chunk shape: shape_prepare builds them
+        b->filters[static_cast<size_t>(f)] =
+            IirBatchFilter{static_cast<float>(gain), ns, static_cast<int>(b->sec32.size()), 0};
+        for (int k = 0; k < ns; ++k) b->sec32.push_back(s32[k]);
         // tail-aggregate schedule: pieces for the cascade's state to decay, and Phi^512
         std::vector<float> pf;
         b->tail_need[static_cast<size_t>(f)] = tail_pieces(s32, ns, IIR_TAIL_MAX_PIECES, pf);
@@ -656,8 +650,6 @@ int iir_batch_create(iir_batch** out, const float* sos, const int* n_sections, i
     b->shape_data.resize(shapes().size());
     int st = cuda_status(cudaGetDevice(&b->device));
     if (!st) st = cuda_status(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
-    if (!st) st = cuda_status(cudaMalloc(&b->d_secs, secs.size() * sizeof(IirSection)));
-    if (!st) st = cuda_status(cudaMemcpy(b->d_secs, secs.data(), secs.size() * sizeof(IirSection), cudaMemcpyHostToDevice));
     if (!st) st = cuda_status(cudaMalloc(&b->d_phi, phi.size() * sizeof(float)));
     if (!st) st = cuda_status(cudaMemcpy(b->d_phi, phi.data(), phi.size() * sizeof(float), cudaMemcpyHostToDevice));
     if (!st) st = cuda_status(cudaMalloc(&b->d_state, sizeof(IirLaunchState)));

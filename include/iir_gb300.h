@@ -82,8 +82,21 @@ int iir_sos_filter(const float* x, float* y, size_t n, const float* sos, int n_s
                    int kernel, void* stream);
 
 /* Same as iir_sos_filter with an explicit BLOCK_SIZE x N_BLOCKS geometry
- * (reference: -DBLOCK_SIZE / -DN_BLOCKS, run_performance.sh:22-60). For PLR, block_size is
- * the thread-block size and n_blocks the values per thread (PLR_X, plr_kernels.cuh:94-101). */
+ * (reference: -DBLOCK_SIZE / -DN_BLOCKS, run_performance.sh:22-60), block_size in {32, 64},
+ * n_blocks in {16, 32, 64, 128}; other values give IIR_ERR_UNSUPPORTED.
+ *   - n_blocks is the samples per row (one reference thread's samples).
+ *   - STCR / DTCR: block_size is the height of a cyclic-reduction tile in rows, as the
+ *     reference's thread block is: STCR has one thread per row (one warp per tile at 32, two
+ *     at 64), DTCR two (two warps at 32, four at 64); the warps of a tile pass each level's
+ *     boundary rows through shared memory (stcr_kernels.cuh:2586-3605,
+ *     dtcr_kernels.cuh:2500-3521).
+ *   - PH: block_size 32 and 64 run the same kernel, whose row scan already spans all rows of
+ *     the chunk (warp scans joined across warps), the reference's PH_32 and PH_64 block scans
+ *     alike (ph_kernels.cuh:208, 501).
+ *   - A block filters a chunk of whole tiles (32 to 256 rows); the chunk, not one tile, is
+ *     the unit of the lookback.
+ * For PLR, block_size is the thread-block size and n_blocks the values per thread (PLR_X,
+ * plr_kernels.cuh:94-101). */
 int iir_sos_filter_geom(const float* x, float* y, size_t n, const float* sos, int n_sections,
                         int kernel, int block_size, int n_blocks, void* stream);
 

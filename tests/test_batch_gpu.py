@@ -184,11 +184,22 @@ def test_bound_batch_replays_in_a_cuda_graph(cuda_device):
     bound.close()
 
 
+def _resonator(w, r):
+    """Band-pass biquad with poles r e^(+-i pi w): its state decays as r^n."""
+    g = (1.0 - r * r) / 2.0
+    return np.array([[g, 0.0, -g, 1.0, -2.0 * r * np.cos(np.pi * w), r * r]])
+
+
 def _mixed_filters():
-    """Filters on both schedules: most decay within half a chunk (tail aggregate); butter(2, 0.003)
-    and butter(16, 0.05) do not at any shape (per-section lookback)."""
+    """Filters on both schedules. Most decay within half a chunk (tail aggregate). Two take the
+    per-section lookback at every shape: a resonator of pole radius 0.996 (12 pieces of 512
+    samples to decay to 1e-10, more than the 8 the schedule allows) alone and behind a
+    butter(14, 0.6). Their poles are away from z = 1, so float32 filters them as well as any
+    other filter here (a sequential float32 cascade is within 2e-6 RMS of FP64); a low-cutoff
+    filter with the same decay, butter(2, 0.003), is not (1.7e-4 sequentially)."""
     from scipy import signal
-    return _filters() + [(2, signal.butter(2, 0.003, output="sos")), (16, signal.butter(16, 0.05, output="sos"))]
+    res = _resonator(0.5, 0.996)
+    return _filters() + [(2, res), (16, np.vstack([signal.butter(14, 0.6, output="sos"), res]))]
 
 
 @pytest.mark.parametrize("shape", [(128, 64), (128, 32), (128, 16), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
@@ -283,8 +294,8 @@ def test_tune_batch_picks_a_shape_and_filters_correctly(cuda_device):
     res = autotune.tune_batch(batch, x, y, off, flt, reps=2)
     assert len(res["table"]) == 4 and all(t["gsps"] > 0 for t in res["table"])
     assert [batch.shape()["rows"], batch.shape()["samples_per_row"]] == res["shape"]
-    # short segments: the model ranks the small chunks first (less padding)
-    assert res["model_order"][0][0] * res["model_order"][0][1] <= 2048
+    # short segments: the model ranks the biggest chunk, mostly padding here, last
+    assert res["model_order"][-1] == [128, 64]
     batch.packed(x, y, off, flt)
     batch.check()
     yh = y.cpu().numpy()
