@@ -716,14 +716,54 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     print(json.dumps(out), flush=True)
 
 
+def run_only_batch(args, spec: str) -> None:
+    """The batching form alone (a short command to profile its kernel): the mixed multichannel
+    workload with channel lengths scaled by 2^(LOG2N - 28) (at least 64 samples each), chunk shape
+    ROWSxN (default 128x64), a bound segment table launched args.steps times after args.warmup."""
+    import numpy as np
+    import torch
+
+    import cuda_recursive_filtering_gb300 as pkg
+    from cuda_recursive_filtering_gb300 import Batch, workloads
+    parts = spec.split(":")
+    rows, n_per_row = (int(v) for v in parts[1].split("x")) if len(parts) > 1 else (128, 64)
+    pkg.load_library()
+    dev = torch.device("cuda", 0)
+    filters, lens = workloads.multichannel_mixed()
+    lens = np.maximum(64, (lens.astype(np.float64) * 2.0 ** (LOG2N - 28)).astype(np.int64))
+    batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 1024 + len(filters)), device=dev)
+    batch.set_shape(rows, n_per_row)
+    off = np.concatenate([[0], np.cumsum(lens)])
+    x = workloads.uniform_signal(int(off[-1]), 3, device=dev)
+    y = torch.empty_like(x)
+    bound = batch.bind(x, y, off, np.arange(len(filters), dtype=np.int32))
+    for _ in range(args.warmup):
+        bound()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+    s.record()
+    for _ in range(args.steps):
+        bound()
+    e.record()
+    torch.cuda.synchronize()
+    batch.check()
+    ms = s.elapsed_time(e) / args.steps
+    print(json.dumps({"only": spec, "shape": batch.shape(), "samples": int(off[-1]), "ms_per_launch": ms,
+                      "gsps": round(float(off[-1]) / (ms * 1e-3) / 1e9, 1)}), flush=True)
+
+
 def run_only(args, spec: str) -> None:
     """One realization / order / geometry on the plain workload at 2^LOG2N samples, timed like the
-    headline and nothing else (a short command to profile one kernel): spec = KERNEL:ORDER[:BxN]."""
+    headline and nothing else (a short command to profile one kernel): spec = KERNEL:ORDER[:BxN],
+    or BATCH[:ROWSxN] for the batching form (run_only_batch)."""
     import torch
     from scipy import signal
 
     import cuda_recursive_filtering_gb300 as pkg
     from cuda_recursive_filtering_gb300 import Plan, workloads
+    if spec.split(":")[0] == "BATCH":
+        run_only_batch(args, spec)
+        return
     parts = spec.split(":")
     kernel, order = parts[0], int(parts[1])
     b, nb = (int(v) for v in parts[2].split("x")) if len(parts) > 2 else (0, 0)
@@ -749,7 +789,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
-    ap.add_argument("--only", default=None, metavar="KERNEL:ORDER[:BxN]",
+    ap.add_argument("--only", default=None, metavar="KERNEL:ORDER[:BxN] | BATCH[:ROWSxN]",
                     help="time one realization / order / geometry and print only that (for profiling)")
     args = ap.parse_args()
     globals()["LOG2N"] = args.log2n
