@@ -48,9 +48,26 @@ constexpr int TC_NACC = 3;                // TMEM accumulators (tiles in flight 
 constexpr int TC_NS = TC_NACC;            // aggregate / X hand-off slots
 constexpr int TC_NXH = TC_NACC + 2;       // input-history slots
 constexpr int TC_XCOL = 256;              // TMEM columns of the x operand: 2 buffers x [hi 64 | lo 64]
-constexpr int TC_GROUPS = 16;             // scan sub-blocks (half-warps)
-constexpr int TC_SUB = TC_NB / TC_GROUPS;  // chunks per sub-block
 constexpr int TC_DMAX = 16;               // carried states (order <= 16)
+constexpr int TC_GROUPS_MAX = 32;         // most scan sub-blocks of a tile
+constexpr int TC_LEVELS_MAX = 5;          // most combine levels (log2 of the sub-blocks)
+
+// The scans of a tile's 128 chunks: each compute group splits them into sub-blocks, scanned in
+// parallel by LG lanes each (lane = state component), then joined by a Kogge-Stone combine over
+// the sub-blocks with Phi^(SUB 2^l). Fewer states need fewer lanes, so a cascade of up to 8 states
+// runs twice the sub-blocks at half the length (32 x 4 chunks, 5 combine levels) where 16 states
+// take 16 x 8 chunks and 4 levels: the scan and rescan, the kernel's serial CUDA-core phases, take
+// half the steps.
+template <int KD>
+struct TcScan {
+    static constexpr int LG = KD <= 8 ? 8 : 16;  // lanes per sub-block
+    static constexpr int GROUPS = TC_CW * 32 / LG;
+    static constexpr int SUB = TC_NB / GROUPS;   // chunks per sub-block
+    static constexpr int LEVELS = GROUPS == 32 ? 5 : 4;
+    static_assert(KD <= LG && GROUPS <= TC_GROUPS_MAX && LEVELS <= TC_LEVELS_MAX && (1 << LEVELS) == GROUPS, "scan shape");
+    static_assert(2 * SUB <= LG, "one lane per history column of a sub-block's chunks");
+};
+constexpr int tc_scan_sub(int kd) { return kd <= 8 ? 4 : 8; }  // TcScan<KD>::SUB, for the host
 constexpr int TC_N1 = 80;                 // GEMM 1 N: 64 outputs + 16 end states
 constexpr int TC_N2 = 64;                 // GEMM 2 N: 64 outputs
 constexpr int TC_ACC = 80;                // TMEM columns per accumulator
@@ -71,7 +88,7 @@ struct TcParams {
     const float* h2img;          // GEMM 2 B operand [H | Hx]: [hi, lo] x TC_H2B
     const float* phi;            // 16 x 16 (row-major, zero beyond D)
     const float* phix;           // 16 x 2
-    const float* phi_pow;        // Phi^(8 * 2^b), b < 4: [b][e / 4][d][e % 4] = P[d][e]
+    const float* phi_pow;        // Phi^(SUB * 2^b), b < TC_LEVELS_MAX: [b][e / 4][d][e % 4] = P[d][e]
     const float* pc;             // Q^l (l <= 32), KD x KD
     const float* pg;             // Q^(32 l) (l <= 32), KD x KD
     long long timeout_ns;
@@ -94,9 +111,9 @@ struct TcAux {
     int pad;
     float agg[TC_NS][TC_DMAX];       // tile aggregate (zero incoming state), for the lookback warp
     float X[TC_NS][TC_DMAX];         // incoming state of the tile, from the lookback warp
-    float Ig0[TC_NACC][TC_GROUPS][TC_DMAX];  // zero-start incoming state of each sub-block, per tile
+    float Ig0[TC_NACC][TC_GROUPS_MAX][TC_DMAX];  // zero-start incoming state of each sub-block, per tile
     float xh[TC_NXH][TC_NB][2];      // input history of each chunk, per tile
-    alignas(16) float phip[4][TC_DMAX / 4][TC_DMAX][4];  // Phi^(8 * 2^b): [b][e / 4][d][e % 4] = P[d][e]
+    alignas(16) float phip[TC_LEVELS_MAX][TC_DMAX / 4][TC_DMAX][4];  // Phi^(SUB 2^b): [b][e / 4][d][e % 4] = P[d][e]
 };
 
 struct TcSmem {
@@ -105,9 +122,9 @@ struct TcSmem {
     static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target)
     static constexpr size_t A2S = XS + 4 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
     static constexpr size_t SCRF = A2S + 2 * TC_KB * 4;         // front scratch: end-state rows, combine
-    static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS * TC_DMAX) * 4;
+    static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS_MAX * TC_DMAX) * 4;
     static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, states, patches
-    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS * TC_DMAX + TC_CW * 32 * 8) * 4;
+    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS_MAX * TC_DMAX + TC_CW * 32 * 8) * 4;
     static constexpr size_t AUX = (SCRB + SCRB_BYTES + 15) / 16 * 16;
     static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
 };
@@ -331,7 +348,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         float4* z = reinterpret_cast<float4*>(a2s);
         for (int i = tid; i < TC_KB / 2; i += TC_THREADS) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // 2 x TC_KB
         float* pp = &aux->phip[0][0][0][0];
-        for (int i = tid; i < 4 * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
+        for (int i = tid; i < TC_LEVELS_MAX * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
     }
     if (warp == TC_MW) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&aux->tmem)),
@@ -497,16 +514,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         const int cw = warp - TC_CW0;
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int hh = cw >> 2;                 // which of the two warps on the quadrant
-        const int grp = ct >> 4, d = ct & 15;   // scan: sub-block, state component
+        using Scan = TcScan<KD>;
+        const int grp = ct / Scan::LG, d = ct % Scan::LG;  // scan: sub-block, state component
         float phi_row[KD], phix0, phix1;
 #pragma unroll
         for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
         phix0 = __ldg(p.phix + d * 2);
         phix1 = __ldg(p.phix + d * 2 + 1);
         float* U = reinterpret_cast<float*>(base + TcSmem::SCRF);  // [128][TC_UP] end-state rows
-        float* V0 = U + TC_NB * TC_UP;                             // [16][16] x 2 combine ping-pong
-        float* V1 = V0 + TC_GROUPS * TC_DMAX;
-        float* SB = V1 + TC_GROUPS * TC_DMAX;                      // [16][16] scan state broadcast
+        float* V0 = U + TC_NB * TC_UP;                             // [groups][16] x 2 combine ping-pong
+        float* V1 = V0 + TC_GROUPS_MAX * TC_DMAX;
+        float* SB = V1 + TC_GROUPS_MAX * TC_DMAX;                  // [groups][16] scan state broadcast
         uint32_t tma_par[2] = {0u, 0u}, tma_real[2] = {0u, 0u}, g1_par = 0;
 
         auto bulk = [&](uint32_t kk) {
@@ -538,7 +556,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             return (s0 + s1) + (s2 + s3);
         };
-        auto mv_smem = [&](int b, const float* v) {  // (Phi^(8 * 2^b) v)_d, v a 16-byte aligned smem vector
+        auto mv_smem = [&](int b, const float* v) {  // (Phi^(SUB * 2^b) v)_d, v a 16-byte aligned smem vector
             const float4* m4 = reinterpret_cast<const float4*>(&aux->phip[b][0][d][0]);
             const float4* v4 = reinterpret_cast<const float4*>(v);
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
@@ -664,16 +682,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             if (ct == 0) TC_STAMP(k, 2);
             const float* xhk = &aux->xh[k % TC_NXH][0][0];
             float S = 0.f;
-            for (int i = 0; i < TC_SUB; ++i)
-                S = step(S, grp * TC_SUB + i, xhk + (grp * TC_SUB + i) * 2, SB + grp * TC_DMAX);
+            for (int i = 0; i < Scan::SUB; ++i)
+                S = step(S, grp * Scan::SUB + i, xhk + (grp * Scan::SUB + i) * 2, SB + grp * TC_DMAX);
             V0[grp * TC_DMAX + d] = S;
             if (ct == 0) TC_STAMP(k, 3);
             bar_group(1);
-            // inclusive scan over the sub-blocks: V_g += Phi^(8 s) V_(g-s), s = 1, 2, 4, 8
+            // inclusive scan over the sub-blocks: V_g += Phi^(SUB s) V_(g-s), s = 1, 2, 4, ...
             float* Vc = V0;
             float* Vn = V1;
 #pragma unroll
-            for (int l = 0; l < 4; ++l) {
+            for (int l = 0; l < Scan::LEVELS; ++l) {
                 const int s = 1 << l;
                 float a = Vc[grp * TC_DMAX + d];
                 if (grp >= s) a += mv_smem(l, Vc + (grp - s) * TC_DMAX);
@@ -685,7 +703,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             if (ct == 0) TC_STAMP(k, 4);
             aux->Ig0[k % TC_NACC][grp][d] = grp > 0 ? Vc[(grp - 1) * TC_DMAX + d] : 0.f;
-            if (grp == TC_GROUPS - 1) aux->agg[k % TC_NS][d] = Vc[grp * TC_DMAX + d];
+            if (grp == Scan::GROUPS - 1) aux->agg[k % TC_NS][d] = Vc[grp * TC_DMAX + d];
             bar_group(1);
             if (ct < KD / 2) {  // the aggregate's part words, one pair per lane
                 const uint32_t t = tile_of(k);
@@ -717,7 +735,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         const int cw = warp - TC_CW0 - TC_CW;
         const int q = warp & 3;
         const int hh = cw >> 2;
-        const int grp = ct >> 4, d = ct & 15;
+        using Scan = TcScan<KD>;
+        const int grp = ct / Scan::LG, d = ct % Scan::LG;  // scan: sub-block, state component
         float phi_row[KD], phix0, phix1;
 #pragma unroll
         for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
@@ -745,7 +764,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             return (s0 + s1) + (s2 + s3);
         };
-        auto mv_smem = [&](int b, const float* v) {  // (Phi^(8 * 2^b) v)_d, v a 16-byte aligned smem vector
+        auto mv_smem = [&](int b, const float* v) {  // (Phi^(SUB * 2^b) v)_d, v a 16-byte aligned smem vector
             const float4* m4 = reinterpret_cast<const float4*>(&aux->phip[b][0][d][0]);
             const float4* v4 = reinterpret_cast<const float4*>(v);
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
@@ -760,10 +779,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             return (s0 + s1) + (s2 + s3);
         };
         float* vx = VX + grp * TC_DMAX;                  // the group's state buffer
-        float4* patch = reinterpret_cast<float4*>(VX + TC_GROUPS * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
+        float4* patch = reinterpret_cast<float4*>(VX + TC_GROUPS_MAX * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
         float xin = 0.f;
-        // c1. tile kk: the lookback's X, end-state rows from TMEM, Phi^(8 grp) X (a product of
-        // Phi^(8 * 2^b) over the bits of grp); runs while GEMM 2 of the tile before is in flight
+        // c1. tile kk: the lookback's X, end-state rows from TMEM, Phi^(SUB grp) X (a product of
+        // Phi^(SUB * 2^b) over the bits of grp); runs while GEMM 2 of the tile before is in flight
         auto prepare = [&](uint32_t kk) {
             const int sl = kk % TC_NS;
             if (!tc_wait(&aux->mb_x[sl], (kk / TC_NS) & 1u, wait_lim, &aux->bail))
@@ -779,7 +798,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             vx[d] = aux->X[sl][d];
             __syncwarp();
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
+            for (int b = 0; b < Scan::LEVELS; ++b) {
                 const float w = mv_smem(b, vx);
                 __syncwarp();
                 if ((grp >> b) & 1) vx[d] = w;
@@ -793,8 +812,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             if (ct == 0) TC_STAMP(kk, 9);
             const float* xhp = &aux->xh[kk % TC_NXH][0][0];
             float S = aux->Ig0[kk % TC_NACC][grp][d] + xin;
-            for (int i = 0; i < TC_SUB; ++i) {
-                const int j = grp * TC_SUB + i;
+            for (int i = 0; i < Scan::SUB; ++i) {
+                const int j = grp * Scan::SUB + i;
                 if (d < D) {
                     const float h = tf32_hi(S);
                     a2s[swz32(j, d)] = h;
@@ -807,8 +826,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 }
                 S = step(S, j, xhp + j * 2, vx);
             }
-            if (D + 2 > 16) {  // D = 16: history columns 16, 17 of the 8 chunks, one per lane
-                const int j = grp * TC_SUB + (d >> 1), e = d & 1;
+            if (D + 2 > Scan::LG) {  // D = LG: history columns D, D + 1 of the sub-block's chunks, one per lane
+                const int j = grp * Scan::SUB + (d >> 1), e = d & 1;
                 const float v = xhp[j * 2 + e];
                 const float h = tf32_hi(v);
                 a2s[swz32(j, D + e)] = h;
@@ -1248,13 +1267,14 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
             img2[TC_H2B + swz32h(m, c)] = tf32_hi_h(v - hv);
         }
     const int KD = t->KD;
-    std::vector<float> phi(TC_DMAX * TC_DMAX), phix(TC_DMAX * 2), ppow(static_cast<size_t>(4) * TC_DMAX * TC_DMAX),
+    std::vector<float> phi(TC_DMAX * TC_DMAX), phix(TC_DMAX * 2), ppow(static_cast<size_t>(iirgb::TC_LEVELS_MAX) * TC_DMAX * TC_DMAX),
         pc(static_cast<size_t>(33) * KD * KD), pg(static_cast<size_t>(33) * KD * KD);
     for (size_t i = 0; i < phi.size(); ++i) phi[i] = static_cast<float>(Phi[i]);
     for (size_t i = 0; i < phix.size(); ++i) phix[i] = static_cast<float>(Phix[i]);
     {
-        Mat P = matpow(Phi, 8, TC_DMAX);  // Phi^(8 * 2^b), stored [b][e / 4][d][e % 4] = P[d][e]
-        for (int b = 0; b < 4; ++b) {
+        // Phi^(SUB * 2^b), stored [b][e / 4][d][e % 4] = P[d][e] (SUB = the kernel's sub-block length)
+        Mat P = matpow(Phi, iirgb::tc_scan_sub(KD), TC_DMAX);
+        for (int b = 0; b < iirgb::TC_LEVELS_MAX; ++b) {
             for (int dd = 0; dd < TC_DMAX; ++dd)
                 for (int e = 0; e < TC_DMAX; ++e)
                     ppow[((static_cast<size_t>(b) * (TC_DMAX / 4) + e / 4) * TC_DMAX + dd) * 4 + e % 4] =
