@@ -717,20 +717,28 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
 
 
 def run_only_batch(args, spec: str) -> None:
-    """The batching form alone (a short command to profile its kernel): the mixed multichannel
-    workload with channel lengths scaled by 2^(LOG2N - 28) (at least 64 samples each), chunk shape
-    ROWSxN (default 128x64), a bound segment table launched args.steps times after args.warmup."""
+    """The batching form alone (a short command to profile its kernel): BATCH[:ROWSxN] is the mixed
+    multichannel workload with channel lengths scaled by 2^(LOG2N - 28) (at least 64 samples each),
+    BATCH1:ORDER[:ROWSxN] one segment of 2^LOG2N samples with butter(ORDER, 0.1); chunk shape ROWSxN
+    (default 128x64), a bound segment table launched args.steps times after args.warmup."""
     import numpy as np
     import torch
 
     import cuda_recursive_filtering_gb300 as pkg
     from cuda_recursive_filtering_gb300 import Batch, workloads
     parts = spec.split(":")
-    rows, n_per_row = (int(v) for v in parts[1].split("x")) if len(parts) > 1 else (128, 64)
+    single = parts[0] == "BATCH1"  # BATCH1:ORDER[:ROWSxN]: one segment of 2^LOG2N, butter(ORDER, 0.1)
+    k = 2 if single else 1
+    shape_part = parts[k] if len(parts) > k else None
+    rows, n_per_row = (int(v) for v in shape_part.split("x")) if shape_part else (128, 64)
     pkg.load_library()
     dev = torch.device("cuda", 0)
-    filters, lens = workloads.multichannel_mixed()
-    lens = np.maximum(64, (lens.astype(np.float64) * 2.0 ** (LOG2N - 28)).astype(np.int64))
+    if single:
+        from scipy import signal
+        filters, lens = [signal.butter(int(parts[1]), 0.1, output="sos")], np.array([1 << LOG2N], dtype=np.int64)
+    else:
+        filters, lens = workloads.multichannel_mixed()
+        lens = np.maximum(64, (lens.astype(np.float64) * 2.0 ** (LOG2N - 28)).astype(np.int64))
     batch = Batch(filters, max_segments=len(filters), max_chunks=int(lens.sum() // 1024 + len(filters)), device=dev)
     batch.set_shape(rows, n_per_row)
     off = np.concatenate([[0], np.cumsum(lens)])
@@ -761,7 +769,7 @@ def run_only(args, spec: str) -> None:
 
     import cuda_recursive_filtering_gb300 as pkg
     from cuda_recursive_filtering_gb300 import Plan, workloads
-    if spec.split(":")[0] == "BATCH":
+    if spec.split(":")[0] in ("BATCH", "BATCH1"):
         run_only_batch(args, spec)
         return
     parts = spec.split(":")
@@ -789,7 +797,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--log2n", type=int, default=LOG2N,
                     help="signal length 2^k (the bench line is quoted at 2^28; smaller k is for profiling)")
-    ap.add_argument("--only", default=None, metavar="KERNEL:ORDER[:BxN] | BATCH[:ROWSxN]",
+    ap.add_argument("--only", default=None, metavar="KERNEL:ORDER[:BxN] | BATCH[:ROWSxN] | BATCH1:ORDER[:ROWSxN]",
                     help="time one realization / order / geometry and print only that (for profiling)")
     args = ap.parse_args()
     globals()["LOG2N"] = args.log2n
