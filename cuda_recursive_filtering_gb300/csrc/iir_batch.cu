@@ -229,15 +229,7 @@ struct BatchBlock {
             }
             xh2 *= gain;
             xh1 *= gain;
-            named_barrier_rows(NW);
-            if (live && gain != 1.f) {
-#pragma unroll 4
-                for (int j = 0; j < N / 4; ++j) {
-                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
-                    const float4 v = *ptr;
-                    *ptr = make_float4(v.x * gain, v.y * gain, v.z * gain, v.w * gain);
-                }
-            }
+            named_barrier_rows(NW);  // histories read before the first pass overwrites rows (it applies the gain)
         }
         // positions of the segment's last two samples relative to this chunk
         const long long m1 = nrem - 1, m2 = nrem - 2;  // in [0, CHUNK) when inside this chunk
@@ -250,7 +242,8 @@ struct BatchBlock {
             float s0 = 0.f, s1 = 0.f, in0 = 0.f, in1 = 0.f;
             if (live) {
                 if (sec == 0)
-                    Ph::template filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1);
+                    Ph::template filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1,
+                                                    gain);
                 else
                     Ph::template filter_pass<true>(buf, r, q.b1, q.b2, q.a1, q.a2, pa1, pa2, d2, d1, xh2, xh1, s0, s1);
                 warp_scan2<32, 1>(s0, s1, q.M, lane);

@@ -50,13 +50,13 @@ struct PhBlock {
     }
 
     // One pass over the row: x = stored value (+ correction of the previous section, whose
-    // recurrence is (pa1, pa2) and whose incoming state is (d2, d1)), then FIR + recurrence
-    // with zero row state; the zero-state output overwrites the row. Returns the row's
-    // zero-state tail pair in (s0, s1).
+    // recurrence is (pa1, pa2) and whose incoming state is (d2, d1); or, for the first section,
+    // times the cascade's input gain g), then FIR + recurrence with zero row state; the
+    // zero-state output overwrites the row. Returns the row's zero-state tail pair in (s0, s1).
     template <bool CORRECT>
     __device__ static void filter_pass(float* buf, int r, float b1, float b2, float a1, float a2, float pa1,
                                        float pa2, float d2, float d1, float& xh2, float& xh1, float& s0,
-                                       float& s1) {
+                                       float& s1, float g = 1.f) {
         float y1 = 0.f, y2 = 0.f;
 #pragma unroll
         for (int j = 0; j < N / 4; ++j) {
@@ -72,6 +72,8 @@ struct PhBlock {
                     d2 = d1;
                     d1 = dn;
                     xv += dn;
+                } else {
+                    xv *= g;
                 }
                 const float wv = fmaf(b2, xh2, fmaf(b1, xh1, xv));
                 const float y = fmaf(a1, y1, fmaf(a2, y2, wv));
@@ -128,16 +130,9 @@ struct PhBlock {
             }
             xh2 *= gain;
             xh1 *= gain;
-            // Every row has read its neighbour's history before any row is overwritten.
+            // Every row has read its neighbour's history before any row is overwritten (the
+            // first section's pass applies the gain as it reads the raw samples).
             named_barrier_rows(NW);
-            if (gain != 1.f) {
-#pragma unroll 4
-                for (int j = 0; j < N / 4; ++j) {
-                    float4* ptr = reinterpret_cast<float4*>(buf + swz<N, ROWS, true>(r, 4 * j));
-                    const float4 q = *ptr;
-                    *ptr = make_float4(q.x * gain, q.y * gain, q.z * gain, q.w * gain);
-                }
-            }
         }
         float pa1 = 0.f, pa2 = 0.f, d2 = 0.f, d1 = 0.f;  // previous section's correction
         for (int sec = 0; sec < p.n_sections; ++sec) {
@@ -147,7 +142,7 @@ struct PhBlock {
             float s0 = 0.f, s1 = 0.f, in0 = 0.f, in1 = 0.f;
             if (row_warp) {
                 if (sec == 0)
-                    filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1);
+                    filter_pass<false>(buf, r, q.b1, q.b2, q.a1, q.a2, 0.f, 0.f, 0.f, 0.f, xh2, xh1, s0, s1, gain);
                 else
                     filter_pass<true>(buf, r, q.b1, q.b2, q.a1, q.a2, pa1, pa2, d2, d1, xh2, xh1, s0, s1);
                 // scan of row tails (zero block state)
