@@ -60,7 +60,8 @@ constexpr int TC_LEVELS_MAX = 5;          // most combine levels (log2 of the su
 // half the steps.
 template <int KD>
 struct TcScan {
-    static constexpr int LG = KD <= 8 ? 8 : 16;  // lanes per sub-block
+    static constexpr int LG_SHIFT = KD <= 8 ? 3 : 4;
+    static constexpr int LG = 1 << LG_SHIFT;  // lanes per sub-block
     static constexpr int GROUPS = TC_CW * 32 / LG;
     static constexpr int SUB = TC_NB / GROUPS;   // chunks per sub-block
     static constexpr int LEVELS = GROUPS == 32 ? 5 : 4;
@@ -102,7 +103,9 @@ struct TcParams {
     unsigned long long* prof;
 };
 
-struct TcAux {
+template <int G>
+struct TcAuxG {
+    static constexpr int LEVELS = G == 32 ? 5 : 4;
     unsigned long long mb_tma[2], mb_g1[2], mb_g2, mb_split[2], mb_sready, mb_accfree, mb_agg[TC_NS], mb_x[TC_NS];
     uint32_t tmem;
     uint32_t epoch;
@@ -111,27 +114,31 @@ struct TcAux {
     int pad;
     float agg[TC_NS][TC_DMAX];       // tile aggregate (zero incoming state), for the lookback warp
     float X[TC_NS][TC_DMAX];         // incoming state of the tile, from the lookback warp
-    float Ig0[TC_NACC][TC_GROUPS_MAX][TC_DMAX];  // zero-start incoming state of each sub-block, per tile
+    float Ig0[TC_NACC][G][TC_DMAX];  // zero-start incoming state of each sub-block, per tile
     float xh[TC_NXH][TC_NB][2];      // input history of each chunk, per tile
-    alignas(16) float phip[TC_LEVELS_MAX][TC_DMAX / 4][TC_DMAX][4];  // Phi^(SUB 2^b): [b][e / 4][d][e % 4] = P[d][e]
+    alignas(16) float phip[LEVELS][TC_DMAX / 4][TC_DMAX][4];  // Phi^(SUB 2^b): [b][e / 4][d][e % 4] = P[d][e]
 };
 
-struct TcSmem {
+// Shared-memory layout for a scan of G sub-blocks (TcScan<KD>::GROUPS): only the scratch areas of
+// the two compute groups depend on it.
+template <int G>
+struct TcSmemG {
     static constexpr size_t B1 = 0;                             // 4 x TC_B1KB floats
     static constexpr size_t H2 = B1 + 4 * TC_B1KB * 4;          // 2 x TC_H2B
     static constexpr size_t XS = H2 + 2 * TC_H2B * 4;           // 2 stages x 2 k-blocks x TC_KB (TMA target)
     static constexpr size_t A2S = XS + 4 * TC_KB * 4;           // state operand [hi, lo] x TC_KB
     static constexpr size_t SCRF = A2S + 2 * TC_KB * 4;         // front scratch: end-state rows, combine
-    static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * TC_GROUPS_MAX * TC_DMAX) * 4;
+    static constexpr size_t SCRF_BYTES = (TC_NB * TC_UP + 3 * G * TC_DMAX) * 4;
     static constexpr size_t SCRB = SCRF + SCRF_BYTES;           // back scratch: end-state rows, states, patches
-    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + TC_GROUPS_MAX * TC_DMAX + TC_CW * 32 * 8) * 4;
+    static constexpr size_t SCRB_BYTES = (TC_NB * TC_UP + G * TC_DMAX + TC_CW * 32 * 8) * 4;
     static constexpr size_t AUX = (SCRB + SCRB_BYTES + 15) / 16 * 16;
-    static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAux);
+    static constexpr size_t BYTES = 1024 + AUX + sizeof(TcAuxG<G>);
+    static_assert(H2 % 1024 == 0 && XS % 1024 == 0 && A2S % 1024 == 0, "operand blocks on the 1024-byte swizzle atom");
+    static_assert(BYTES <= 232448, "shared memory");
 };
-static_assert(TcSmem::H2 % 1024 == 0 && TcSmem::XS % 1024 == 0 && TcSmem::A2S % 1024 == 0,
-              "operand blocks on the 1024-byte swizzle atom");
-static_assert((TC_B1KB * 4) % 1024 == 0 && (TC_H2B * 4) % 1024 == 0, "operand blocks on the swizzle atom");
-static_assert(TcSmem::BYTES <= 232448, "shared memory");
+template <int KD>
+using TcSmem = TcSmemG<TcScan<KD>::GROUPS>;
+constexpr size_t tc_smem_bytes(int kd) { return kd <= 8 ? TcSmemG<32>::BYTES : TcSmemG<16>::BYTES; }
 static_assert(TC_NACC * TC_ACC <= TC_XCOL && TC_XCOL + 256 <= 512, "TMEM columns");
 
 __device__ __forceinline__ int swz32(int r, int c) { return (r << 5) + ((((c >> 2) ^ (r & 7))) << 2) + (c & 3); }
@@ -254,7 +261,8 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* bar, uint32_t parity
     return true;
 }
 // First give-up of the block reports `code`; later ones only stop.
-__device__ __forceinline__ void tc_give_up(TcAux* aux, const TcParams& p, uint32_t epoch, uint32_t code) {
+template <class Aux>
+__device__ __forceinline__ void tc_give_up(Aux* aux, const TcParams& p, uint32_t epoch, uint32_t code) {
     if (atomicExch(&aux->bail, 1) == 0) raise_error(p.state, epoch, code);
 }
 
@@ -326,11 +334,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t a0 = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((a0 + 1023u) & ~1023u) - a0);
-    float* b1 = reinterpret_cast<float*>(base + TcSmem::B1);
-    float* h2 = reinterpret_cast<float*>(base + TcSmem::H2);
-    float* xs = reinterpret_cast<float*>(base + TcSmem::XS);
-    float* a2s = reinterpret_cast<float*>(base + TcSmem::A2S);
-    TcAux* aux = reinterpret_cast<TcAux*>(base + TcSmem::AUX);
+    using Sm = TcSmem<KD>;
+    float* b1 = reinterpret_cast<float*>(base + Sm::B1);
+    float* h2 = reinterpret_cast<float*>(base + Sm::H2);
+    float* xs = reinterpret_cast<float*>(base + Sm::XS);
+    float* a2s = reinterpret_cast<float*>(base + Sm::A2S);
+    using TcAux = TcAuxG<TcScan<KD>::GROUPS>;
+    TcAux* aux = reinterpret_cast<TcAux*>(base + Sm::AUX);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int D = p.D;
     const uint32_t G = gridDim.x;
@@ -348,7 +358,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         float4* z = reinterpret_cast<float4*>(a2s);
         for (int i = tid; i < TC_KB / 2; i += TC_THREADS) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // 2 x TC_KB
         float* pp = &aux->phip[0][0][0][0];
-        for (int i = tid; i < TC_LEVELS_MAX * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
+        for (int i = tid; i < TcAux::LEVELS * TC_DMAX * TC_DMAX; i += TC_THREADS) pp[i] = __ldg(p.phi_pow + i);
     }
     if (warp == TC_MW) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&aux->tmem)),
@@ -515,16 +525,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         const int q = warp & 3;                 // TMEM lane quadrant of this warp
         const int hh = cw >> 2;                 // which of the two warps on the quadrant
         using Scan = TcScan<KD>;
-        const int grp = ct / Scan::LG, d = ct % Scan::LG;  // scan: sub-block, state component
+        const int grp = ct >> Scan::LG_SHIFT, d = ct & (Scan::LG - 1);  // scan: sub-block, state component
         float phi_row[KD], phix0, phix1;
 #pragma unroll
         for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
         phix0 = __ldg(p.phix + d * 2);
         phix1 = __ldg(p.phix + d * 2 + 1);
-        float* U = reinterpret_cast<float*>(base + TcSmem::SCRF);  // [128][TC_UP] end-state rows
+        float* U = reinterpret_cast<float*>(base + Sm::SCRF);      // [128][TC_UP] end-state rows
         float* V0 = U + TC_NB * TC_UP;                             // [groups][16] x 2 combine ping-pong
-        float* V1 = V0 + TC_GROUPS_MAX * TC_DMAX;
-        float* SB = V1 + TC_GROUPS_MAX * TC_DMAX;                  // [groups][16] scan state broadcast
+        float* V1 = V0 + Scan::GROUPS * TC_DMAX;
+        float* SB = V1 + Scan::GROUPS * TC_DMAX;                   // [groups][16] scan state broadcast
         uint32_t tma_par[2] = {0u, 0u}, tma_real[2] = {0u, 0u}, g1_par = 0;
 
         auto bulk = [&](uint32_t kk) {
@@ -736,13 +746,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         const int q = warp & 3;
         const int hh = cw >> 2;
         using Scan = TcScan<KD>;
-        const int grp = ct / Scan::LG, d = ct % Scan::LG;  // scan: sub-block, state component
+        const int grp = ct >> Scan::LG_SHIFT, d = ct & (Scan::LG - 1);  // scan: sub-block, state component
         float phi_row[KD], phix0, phix1;
 #pragma unroll
         for (int e = 0; e < KD; ++e) phi_row[e] = __ldg(p.phi + d * TC_DMAX + e);
         phix0 = __ldg(p.phix + d * 2);
         phix1 = __ldg(p.phix + d * 2 + 1);
-        float* scr = reinterpret_cast<float*>(base + TcSmem::SCRB);
+        float* scr = reinterpret_cast<float*>(base + Sm::SCRB);
         float* U = scr;                                   // [128][TC_UP] end-state rows
         float* VX = scr + TC_NB * TC_UP;                  // [16][16] incoming-state products
         uint32_t g2_par = 0;
@@ -779,7 +789,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             return (s0 + s1) + (s2 + s3);
         };
         float* vx = VX + grp * TC_DMAX;                  // the group's state buffer
-        float4* patch = reinterpret_cast<float4*>(VX + TC_GROUPS_MAX * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
+        float4* patch = reinterpret_cast<float4*>(VX + Scan::GROUPS * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
         float xin = 0.f;
         // c1. tile kk: the lookback's X, end-state rows from TMEM, Phi^(SUB grp) X (a product of
         // Phi^(SUB * 2^b) over the bits of grp); runs while GEMM 2 of the tile before is in flight
@@ -1342,11 +1352,11 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
                 : KD == 8 ? tc_kernel_fn<8>(full)
                           : tc_kernel_fn<16>(full);
         st = cuda_status(cudaFuncSetAttribute(t->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              static_cast<int>(iirgb::TcSmem::BYTES)));
+                                              static_cast<int>(iirgb::tc_smem_bytes(KD))));
     }
     if (!st) {
         int nb = 0;
-        st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, t->fn, iirgb::TC_THREADS, iirgb::TcSmem::BYTES));
+        st = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, t->fn, iirgb::TC_THREADS, iirgb::tc_smem_bytes(KD)));
         if (!st && nb < 1) st = IIR_ERR_UNSUPPORTED;
         t->grid_max = std::max(nb, 1) * t->sms;
     }
@@ -1399,7 +1409,7 @@ int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long tim
     void* args[] = {&q};
     const int grid = static_cast<int>(std::min<size_t>(tiles, static_cast<size_t>(t->grid_max)));
     return cuda_status(cudaLaunchCooperativeKernel(t->fn, dim3(grid), dim3(iirgb::TC_THREADS), args,
-                                                   iirgb::TcSmem::BYTES, stream));
+                                                   iirgb::tc_smem_bytes(t->KD), stream));
 }
 
 namespace {
