@@ -21,10 +21,13 @@
 // (ph_kernels.cuh:265-480), which this replaces by two GEMMs whose cost does not grow with the
 // order (M = L + D rows).
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -169,6 +172,37 @@ __device__ __forceinline__ void umma_tf32_ta(uint32_t tmem, uint32_t ta, uint64_
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem),
         "r"(ta), "l"(db), "r"(idesc), "r"(acc));
+}
+// BF16 operands (kind::f16): D f32, A / B bf16 K-major, M = 128. A from TMEM packs two bf16 per
+// 32-bit column (the lower K index in the low half).
+constexpr uint32_t tc_idesc_bf16(int n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128 >> 4) << 24); }
+constexpr uint32_t TC_IDESC1_BF16 = tc_idesc_bf16(TC_N1);
+__device__ __forceinline__ void umma_bf16_ta(uint32_t tmem, uint32_t ta, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem),
+        "r"(ta), "l"(db), "r"(idesc), "r"(acc));
+}
+// Products of the BF16 split form: BF = 6 takes three parts of each operand (x = b0 + b1 + b2,
+// each the nearest bf16 of what the earlier parts left) and the six products whose parts' ranks
+// sum to at most 2, which keeps float32 accuracy; BF = 3 takes two parts and b0 c0 + b0 c1 + b1 c0.
+template <int BF>
+struct TcBf16 {
+    static constexpr int PARTS = BF == 6 ? 3 : 2;
+    static constexpr int NPROD = BF;
+    __device__ static constexpr int a_part(int i) { return i == 0 ? 0 : i == 1 ? 0 : i == 2 ? 1 : i == 3 ? 0 : i == 4 ? 1 : 2; }
+    __device__ static constexpr int b_part(int i) { return i == 0 ? 0 : i == 1 ? 1 : i == 2 ? 0 : i == 3 ? 2 : i == 4 ? 1 : 0; }
+};
+constexpr int TC_BF_PART_BYTES = TC_N1 * 128;  // one bf16 part of the GEMM 1 B image: 80 rows x 64 bf16
+static_assert(3 * TC_BF_PART_BYTES <= 4 * TC_B1KB * 4 && TC_BF_PART_BYTES % 1024 == 0, "bf16 image in the B1 area");
+__device__ __forceinline__ uint32_t bf16_pair(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);  // .x = lo (low half), .y = hi
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ void tmem_st8u(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(v[0]),
+                 "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
 }
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
     asm volatile(
@@ -329,7 +363,9 @@ __device__ bool lookback_trunc(const TcParams& p, const unsigned long long* slot
 // stages tile k+1 and scans it.
 // FULL: the two-level decoupled lookback (tile transitions that have not decayed); otherwise the
 // truncated lookback, and the two-level code is not compiled in (it would raise register use).
-template <int KD, bool FULL>
+// BF = 0: GEMM 1 in TF32 with the hi / lo split (three products); BF = 3 or 6: GEMM 1 in BF16
+// with the split of TcBf16<BF>. GEMM 2 is TF32 in every form.
+template <int KD, bool FULL, int BF>
 __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_constant__ TcParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     const uint32_t a0 = smem_u32(smem_raw);
@@ -483,17 +519,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                         if (piece == 0) tc_fence_after();
                         const uint32_t xa = tmem + static_cast<uint32_t>(TC_XCOL + (k1 & 1) * 128);  // x hi; lo at + 64
                         const uint32_t dt = tmem + static_cast<uint32_t>((k1 % TC_NACC) * TC_ACC);
-                        const int kb = piece >> 1;
+                        if constexpr (BF == 0) {
+                            const int kb = piece >> 1;
 #pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const int ks = (piece & 1) * 2 + h;
-                            const uint32_t ca = static_cast<uint32_t>(kb * 32 + ks * 8);
-                            const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
-                            const uint64_t bh = umma_desc(smem_u32(b1) + ob);
-                            const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
-                            umma_tf32_ta(dt, xa + ca, bh, TC_IDESC1, (piece == 0 && h == 0) ? 0u : 1u);
-                            umma_tf32_ta(dt, xa + ca, bl, TC_IDESC1, 1u);
-                            umma_tf32_ta(dt, xa + 64 + ca, bh, TC_IDESC1, 1u);
+                            for (int h = 0; h < 2; ++h) {
+                                const int ks = (piece & 1) * 2 + h;
+                                const uint32_t ca = static_cast<uint32_t>(kb * 32 + ks * 8);
+                                const uint32_t ob = (kb * TC_B1KB) * 4 + ks * 32;
+                                const uint64_t bh = umma_desc(smem_u32(b1) + ob);
+                                const uint64_t bl = umma_desc(smem_u32(b1) + 2 * TC_B1KB * 4 + ob);
+                                umma_tf32_ta(dt, xa + ca, bh, TC_IDESC1, (piece == 0 && h == 0) ? 0u : 1u);
+                                umma_tf32_ta(dt, xa + ca, bl, TC_IDESC1, 1u);
+                                umma_tf32_ta(dt, xa + 64 + ca, bh, TC_IDESC1, 1u);
+                            }
+                        } else {
+                            // piece = k-step of 16 samples: x part a at columns 32 a + 8 piece (two bf16
+                            // per column), B part b at b * TC_BF_PART_BYTES + 32 piece bytes
+                            using Bf = TcBf16<BF>;
+#pragma unroll
+                            for (int i = 0; i < Bf::NPROD; ++i) {
+                                const uint32_t ta = xa + static_cast<uint32_t>(32 * Bf::a_part(i) + 8 * piece);
+                                const uint64_t db =
+                                    umma_desc(smem_u32(b1) + static_cast<uint32_t>(Bf::b_part(i) * TC_BF_PART_BYTES + 32 * piece));
+                                umma_bf16_ta(dt, ta, db, TC_IDESC1_BF16, (piece == 0 && i == 0) ? 0u : 1u);
+                            }
                         }
                         if (++piece == 4) {
                             umma_commit(&aux->mb_g1[k1 & 1]);
@@ -620,23 +669,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 const uint32_t xa = tmem + (static_cast<uint32_t>(32 * q) << 16) +
                                     static_cast<uint32_t>(TC_XCOL + (kk & 1) * 128 + 32 * hh);
                 __syncwarp();
+                if constexpr (BF == 0) {
 #pragma unroll
-                for (int half = 0; half < 2; ++half) {
-                    float hi[16], lo[16];
+                    for (int half = 0; half < 2; ++half) {
+                        float hi[16], lo[16];
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const float4 v = row[(4 * half + c) ^ (r & 7)];
-                        hi[4 * c] = tf32_hi(v.x);
-                        hi[4 * c + 1] = tf32_hi(v.y);
-                        hi[4 * c + 2] = tf32_hi(v.z);
-                        hi[4 * c + 3] = tf32_hi(v.w);
-                        lo[4 * c] = tf32_hi(v.x - hi[4 * c]);
-                        lo[4 * c + 1] = tf32_hi(v.y - hi[4 * c + 1]);
-                        lo[4 * c + 2] = tf32_hi(v.z - hi[4 * c + 2]);
-                        lo[4 * c + 3] = tf32_hi(v.w - hi[4 * c + 3]);
+                        for (int c = 0; c < 4; ++c) {
+                            const float4 v = row[(4 * half + c) ^ (r & 7)];
+                            hi[4 * c] = tf32_hi(v.x);
+                            hi[4 * c + 1] = tf32_hi(v.y);
+                            hi[4 * c + 2] = tf32_hi(v.z);
+                            hi[4 * c + 3] = tf32_hi(v.w);
+                            lo[4 * c] = tf32_hi(v.x - hi[4 * c]);
+                            lo[4 * c + 1] = tf32_hi(v.y - hi[4 * c + 1]);
+                            lo[4 * c + 2] = tf32_hi(v.z - hi[4 * c + 2]);
+                            lo[4 * c + 3] = tf32_hi(v.w - hi[4 * c + 3]);
+                        }
+                        tmem_st16(xa + 16 * half, hi);
+                        tmem_st16(xa + 64 + 16 * half, lo);
                     }
-                    tmem_st16(xa + 16 * half, hi);
-                    tmem_st16(xa + 64 + 16 * half, lo);
+                } else {
+                    // bf16 parts of the 32 samples, two per column: part a of k-block hh at columns
+                    // 32 a + 16 hh of the buffer (xa already holds + 32 hh: move it back to the buffer)
+                    const uint32_t xb = xa - static_cast<uint32_t>(32 * hh) + static_cast<uint32_t>(16 * hh);
+#pragma unroll
+                    for (int half = 0; half < 2; ++half) {
+                        uint32_t w[TcBf16<BF>::PARTS][8];
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const float4 v = row[(4 * half + c) ^ (r & 7)];
+                            float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                            for (int a = 0; a < TcBf16<BF>::PARTS; ++a) {
+                                float part[4];
+#pragma unroll
+                                for (int j = 0; j < 4; ++j) {
+                                    part[j] = __bfloat162float(__float2bfloat16_rn(e[j]));
+                                    e[j] -= part[j];
+                                }
+                                w[a][2 * c] = bf16_pair(part[0], part[1]);
+                                w[a][2 * c + 1] = bf16_pair(part[2], part[3]);
+                            }
+                        }
+#pragma unroll
+                        for (int a = 0; a < TcBf16<BF>::PARTS; ++a) tmem_st8u(xb + 32 * a + 8 * half, w[a]);
+                    }
                 }
                 tmem_wait_st();
             }
@@ -945,6 +1022,7 @@ struct TcPlan {
     int D = 0, KD = 0, sms = 0, grid_max = 0;
     bool input_normal = false;  // carried states in the input-normal basis (else balanced)
     int lb_depth = 0;           // truncated lookback depth (0: full decoupled lookback)
+    int bf = 0;                 // GEMM 1 operands: 0 = TF32 hi / lo, 3 or 6 = BF16 split (TcBf16)
     unsigned long long* prof = nullptr;  // timeline buffer (builds with IIR_PROFILE)
     const void* fn = nullptr;
     float* d_tabs = nullptr;  // a1 image, a2 image, phi, phix, phi_grp, pc, pg (one allocation)
@@ -1018,6 +1096,28 @@ Mat matpow(Mat A, unsigned long long e, int n) {
 }
 
 int swz32h(int r, int c) { return (r << 5) + ((((c >> 2) ^ (r & 7))) << 2) + (c & 3); }
+// Nearest bf16 of a finite float (ties to even), and back.
+uint16_t bf16_rn_h(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return static_cast<uint16_t>(u >> 16);
+}
+float bf16_to_f_h(uint16_t h) {
+    const uint32_t u = static_cast<uint32_t>(h) << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+// GEMM 1 operand form of a plan (IIR_GB300_TC_BF16 = 3 or 6 at plan creation): the BF16 split
+// is built for 5..8 and 9..16 carried states with the truncated lookback; every other plan, and
+// the default, uses TF32.
+int tc_bf16_form(int kd, bool full) {
+    const char* e = std::getenv("IIR_GB300_TC_BF16");
+    if (!e || full || kd < 8) return 0;
+    const int v = std::atoi(e);
+    return (v == 3 || v == 6) ? v : 0;
+}
 float tf32_hi_h(float v) {  // nearest TF32 value (as tf32_hi on the device)
     uint32_t u;
     std::memcpy(&u, &v, 4);
@@ -1184,9 +1284,13 @@ bool state_basis(const SectionF32* secs, int K, double gain, std::vector<double>
 }
 
 template <int KD>
-const void* tc_kernel_fn(bool full) {
-    return full ? reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, true>)
-                : reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, false>);
+const void* tc_kernel_fn(bool full, int bf) {
+    if (full) return reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, true, 0>);
+    if constexpr (KD >= 8) {
+        if (bf == 3) return reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, false, 3>);
+        if (bf == 6) return reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, false, 6>);
+    }
+    return reinterpret_cast<const void*>(iirgb::iir_tc_kernel<KD, false, 0>);
 }
 
 }  // namespace
@@ -1311,6 +1415,25 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
             Qm = matmul(Qm, Q, TC_DMAX);
         }
     }
+    // GEMM 1 in BF16 (IIR_GB300_TC_BF16): the B operand image is rebuilt as bf16 parts; part b of
+    // row m, sample c sits at bf16 index b * 80 * 64 + m * 64 + ((c / 8) ^ (m % 8)) * 8 + c % 8
+    // (rows of 128 bytes, 128-byte swizzle)
+    t->bf = tc_bf16_form(t->KD, t->lb_depth == 0);
+    if (t->bf != 0) {
+        std::vector<uint16_t> bimg(static_cast<size_t>(2) * img1.size(), 0);
+        const int parts = t->bf == 6 ? 3 : 2;
+        for (int m = 0; m < TC_N1; ++m)
+            for (int c = 0; c < L; ++c) {
+                float rest = static_cast<float>(A1[m * L + c]);
+                for (int b = 0; b < parts; ++b) {
+                    const uint16_t h = bf16_rn_h(rest);
+                    rest -= bf16_to_f_h(h);
+                    bimg[static_cast<size_t>(b) * (iirgb::TC_BF_PART_BYTES / 2) + m * 64 + (((c >> 3) ^ (m & 7)) << 3) +
+                         (c & 7)] = h;
+                }
+            }
+        std::memcpy(img1.data(), bimg.data(), img1.size() * sizeof(float));
+    }
     const Mat Q32 = matpow(Q, 32, TC_DMAX);
     Mat Pq = identity(TC_DMAX), Pq32 = identity(TC_DMAX);
     for (int l = 0; l <= 32; ++l) {
@@ -1347,10 +1470,10 @@ int tc_plan_create(TcPlan** out, const SectionF32* secs, int K, double gain, siz
     if (!st) st = tc_alloc_carry(t, (std::max<size_t>(max_n, 1) + TC_TILE - 1) / TC_TILE);
     if (!st) {
         const bool full = t->lb_depth == 0;
-        t->fn = KD == 2   ? tc_kernel_fn<2>(full)
-                : KD == 4 ? tc_kernel_fn<4>(full)
-                : KD == 8 ? tc_kernel_fn<8>(full)
-                          : tc_kernel_fn<16>(full);
+        t->fn = KD == 2   ? tc_kernel_fn<2>(full, t->bf)
+                : KD == 4 ? tc_kernel_fn<4>(full, t->bf)
+                : KD == 8 ? tc_kernel_fn<8>(full, t->bf)
+                          : tc_kernel_fn<16>(full, t->bf);
         st = cuda_status(cudaFuncSetAttribute(t->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               static_cast<int>(iirgb::tc_smem_bytes(KD))));
     }

@@ -1,5 +1,6 @@
 """Precision form (IIR_KERNEL_TC): the cascade's chunk solve as tcgen05 TF32 GEMMs with split
-(3-term) products, chunk states joined by a D-dimensional scan and decoupled lookback. Against
+(3-term) products (and GEMM 1 with BF16 split operands), chunk states joined by a D-dimensional
+scan and decoupled lookback. Against
 the FP64 oracle: max|err| <= 1e-4 * max|ref| (the reference's gate, src/test_accuracy.cu:178-188)
 and max|err| / RMS(ref) <= 1e-5 at every order (the precision form's target)."""
 import numpy as np
@@ -110,3 +111,22 @@ def test_tc_cheby1(order, cutoff, cuda_device):
     y = plan(torch.from_numpy(x).cuda())
     plan.check()
     _check(y.cpu().numpy(), x, sos, rms_tol=2e-5)
+
+
+@pytest.mark.parametrize("order", (8, 16))
+@pytest.mark.parametrize("form", ("6", "3"))
+def test_tc_bf16_split_forms(order, form, monkeypatch, cuda_device):
+    """GEMM 1 with BF16 split operands (IIR_GB300_TC_BF16, read when the plan is created) on the
+    precision workload, including ragged sizes. Three parts and six products keep the float32
+    bar (max|err| / RMS <= 1e-5); two parts and three products keep the reference's gate
+    (max|err| <= 1e-4 max|ref|) at about 4e-5 RMS, so their RMS bound here is 1e-4."""
+    from scipy import signal
+    sos = signal.butter(order, 0.05, output="sos")
+    monkeypatch.setenv("IIR_GB300_TC_BF16", form)
+    xt = workloads.noise_plus_tones(1 << 21, 2)
+    plan = Plan(sos, "TC", max_n=xt.numel())
+    monkeypatch.delenv("IIR_GB300_TC_BF16")
+    for n in (xt.numel(), 8192 * 37 + 11, 100):
+        y = plan(xt[:n])
+        plan.check()
+        _check(y.cpu().numpy(), xt[:n].cpu().numpy(), sos, rms_tol=1e-5 if form == "6" else 1e-4)
