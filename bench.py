@@ -126,12 +126,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def time_plan(plan, x, y, steps: int, warmup: int, stream):
+def time_plan(plan, x, y, steps: int, warmup: int, stream, per_launch: bool = False):
+    """ms per launch: the CUDA-event time of `steps` back-to-back launches after `warmup`. With
+    per_launch, every launch is bracketed by its own pair of events and the median launch is
+    returned, so that a host thread descheduled between two launches (the sweep computes its
+    FP64 goldens on host threads meanwhile) leaves the GPU idle outside every timed interval."""
     import torch
     for _ in range(warmup):
         plan(x, y, stream=stream)
     plan.check(stream)
     torch.cuda.synchronize()
+    if per_launch:
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for s, e in ev:
+            s.record(stream)
+            plan(x, y, stream=stream)
+            e.record(stream)
+        torch.cuda.synchronize()
+        plan.check(stream)
+        return statistics.median(s.elapsed_time(e) for s, e in ev)
     s = torch.cuda.Event(enable_timing=True)
     e = torch.cuda.Event(enable_timing=True)
     s.record(stream)
@@ -445,7 +458,7 @@ def run_precision(dev, log2n: int, hbm_gbs: float) -> dict:
                     pl = Plan(sos, "TC" if bf else kname, b, nb, max_n=n, device=dev)
                 finally:
                     os.environ.pop("IIR_GB300_TC_BF16", None)
-                t = time_plan(pl, x, y, 5, 2, stream)
+                t = time_plan(pl, x, y, 5, 2, stream, per_launch=True)
                 pl.check()
                 pl.close()
                 row[kname] = row_entry(n / (t * 1e-3) / 1e9, hbm_gbs, ref.errors(y))
@@ -534,7 +547,7 @@ def run_sweep(dev, x, xh, steps: int, hbm_gbs: float) -> dict:
             for kname, b, nb, key in sweep_keys(order):
                 try:
                     pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
-                    t = time_plan(pl, x, y, max(3, steps // 2), 2, stream)
+                    t = time_plan(pl, x, y, max(3, steps // 2), 2, stream, per_launch=True)
                     rows_full[key] = row_entry(n / (t * 1e-3) / 1e9, hbm_gbs, ref.errors(y))
                     if n25 < n:
                         ms = time_rotating(pl, xs25, ys25, 5, 2 * nbuf, stream)
@@ -612,7 +625,6 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
 
     # ---- headline: device-resident throughput ----
     sos = signal.butter(HEADLINE["order"], 0.1, output="sos")
-    gold = Golden([("headline", sos, xh)], ahead=1)
     plan = Plan(sos, HEADLINE["kernel"], HEADLINE["block_size"], HEADLINE["n_blocks"], max_n=n, device=dev)
     for _ in range(2):
         plan(x, y)
@@ -636,6 +648,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     value = world * n / (ms * 1e-3) / 1e9
     achieved = BYTES_PER_SAMPLE * n / (ms * 1e-3) / 1e9
     # correctness of this exact run: every output of the last timed launch against the oracle
+    # (computed on host threads only now, so that nothing competes with the timed launches)
+    gold = Golden([("headline", sos, xh)], ahead=1)
     head_ref = DeviceRef(gold.get("headline"), dev)
     gold.close()
     chk = head_ref.errors(y)
