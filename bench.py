@@ -157,6 +157,20 @@ def time_plan(plan, x, y, steps: int, warmup: int, stream, per_launch: bool = Fa
     return s.elapsed_time(e) / steps
 
 
+class _RefAsPlan:
+    """A reference kernel module (oracle/refgpu.RefKernel) with the calls time_rotating makes."""
+
+    def __init__(self, rk):
+        self.rk = rk
+
+    def __call__(self, x, y, stream=None):
+        self.rk(x, y, stream)
+
+    def check(self, stream=None):
+        import torch
+        torch.cuda.synchronize()
+
+
 def time_rotating(plan, xs, ys, batches: int, per_batch: int, stream) -> list[float]:
     """The reference's timing method (include/measure.cuh:37-110): launches cycle through
     several identical input / output buffers whose total exceeds L2; `batches` batches of
@@ -539,11 +553,12 @@ def run_sweep(dev, x, xh, steps: int, hbm_gbs: float) -> dict:
     ys25 = [torch.empty(n25, device=dev) for _ in range(nbuf)]
     orders = (2, 4, 8, 16)
     gold = Golden([(o, signal.butter(o, 0.1, output="sos"), xh) for o in orders], ahead=3)
-    rows_full, rows_25 = {}, {}
+    rows_full, rows_25, rows_refk = {}, {}, {}
     try:
         for order in orders:
             s_o = signal.butter(order, 0.1, output="sos")
             ref = DeviceRef(gold.get(order), dev)
+            rows_refk.update(run_reference_kernels(dev, x, y, s_o, order, ref, hbm_gbs, stream))
             for kname, b, nb, key in sweep_keys(order):
                 try:
                     pl = Plan(s_o, kname, b, nb, max_n=n, device=dev)
@@ -561,11 +576,52 @@ def run_sweep(dev, x, xh, steps: int, hbm_gbs: float) -> dict:
         gold.close()
     del xs25, ys25, y
     out = {f"2^{n.bit_length() - 1}": rows_full}
+    for key, row in rows_refk.items():  # the same realization and geometry of this library, and the ratio
+        ours = rows_full.get(key.replace("reference_", ""))
+        if isinstance(row, dict) and isinstance(ours, dict):
+            row["ours_gsps"] = ours["gsps"]
+            row["ours_vs_reference"] = round(ours["gsps"] / row["gsps"], 1)
+    out["reference_kernels"] = rows_refk
     if rows_25:
         out["2^25"] = rows_25
         out["2^25_method"] = (f"{nbuf} identical input and output buffers (> 2x L2) cycled, 5 batches of "
                               f"{2 * nbuf} launches, median batch")
     return out
+
+
+def run_reference_kernels(dev, x, y, sos, order: int, ref, hbm_gbs: float, stream) -> dict:
+    """The reference's own GPU kernels, PH_32 and DTCR_32_UNROLL_64 at 32 x 64
+    (include/ph_kernels.cuh, include/dtcr_kernels.cuh), built from its sources into device code
+    (oracle/refgpu.py) and launched on this GPU under its own launch contract, on the same signal
+    (times the cascade's gain, as its drivers give it) with the same timing as this library's rows;
+    every output against the same FP64 oracle."""
+    import numpy as np
+    import torch
+
+    import oracle
+    from oracle import refgpu
+    if not refgpu.available():
+        return {f"reference_order{order}": "unavailable: the reference kernels' cubins (oracle/_ref) are absent"}
+    sn, g = oracle.normalise_sos(sos)
+    xs = (x * np.float32(g)).contiguous()
+    rows = {}
+    for kname in ("PH", "DTCR_UNROLL"):
+        rk = refgpu.RefKernel(kname, sn, x.numel(), device=dev)
+        for _ in range(3):
+            rk(xs, y)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+        for a, b in ev:
+            a.record(stream)
+            rk(xs, y, stream)
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+        rows[f"reference_order{order}_{kname}_32x64"] = row_entry(x.numel() / (ms * 1e-3) / 1e9, hbm_gbs,
+                                                                  ref.errors(y))
+        rk.close()
+    del xs
+    return rows
 
 
 def run_small(dev, hbm_gbs: float) -> dict:
@@ -601,6 +657,21 @@ def run_small(dev, hbm_gbs: float) -> dict:
         rows[key] = dict(row_entry(n / (p20 * 1e-3) / 1e9, hbm_gbs, e),
                          gsps_median=round(n / (statistics.median(ms) * 1e-3) / 1e9, 1),
                          us_per_launch_p20=round(p20 * 1e3, 2))
+    # the reference's own kernels on the same buffers and timing (oracle/refgpu.py)
+    from oracle import refgpu
+    if refgpu.available():
+        sn, g = oracle.normalise_sos(sos)
+        xsg = [(t * np.float32(g)).contiguous() for t in xs]
+        for kname in ("PH", "DTCR_UNROLL"):
+            rk = refgpu.RefKernel(kname, sn, n, device=dev)
+            ms = time_rotating(_RefAsPlan(rk), xsg, ys, 20, 200, stream)
+            e = oracle.errors(ys[0].cpu().numpy(), ref)
+            rk.close()
+            p20 = sorted(ms)[len(ms) // 5]
+            rows[f"reference_order2_{kname}_32x64"] = dict(
+                row_entry(n / (p20 * 1e-3) / 1e9, hbm_gbs, e),
+                gsps_median=round(n / (statistics.median(ms) * 1e-3) / 1e9, 1), us_per_launch_p20=round(p20 * 1e3, 2))
+        del xsg
     del xs, ys
     return {"rows": rows, "method": f"{nbuf} identical input and output buffers cycled, 20 batches of 200 launches; "
                                     "gsps = 20th-percentile batch, gsps_median = median batch"}
