@@ -590,8 +590,8 @@ def run_sweep(dev, x, xh, steps: int, hbm_gbs: float) -> dict:
 
 
 def run_reference_kernels(dev, x, y, sos, order: int, ref, hbm_gbs: float, stream) -> dict:
-    """The reference's own GPU kernels, PH_32 and DTCR_32_UNROLL_64 at 32 x 64
-    (include/ph_kernels.cuh, include/dtcr_kernels.cuh), built from its sources into device code
+    """The reference's own GPU kernels, PH_32, STCR_32_LOOP, STCR_32_UNROLL_64, DTCR_32_LOOP and
+    DTCR_32_UNROLL_64 (include/{ph,stcr,dtcr}_kernels.cuh), built from its sources into device code
     (oracle/refgpu.py) and launched on this GPU under its own launch contract, on the same signal
     (times the cascade's gain, as its drivers give it) with the same timing as this library's rows;
     every output against the same FP64 oracle."""
@@ -605,7 +605,7 @@ def run_reference_kernels(dev, x, y, sos, order: int, ref, hbm_gbs: float, strea
     sn, g = oracle.normalise_sos(sos)
     xs = (x * np.float32(g)).contiguous()
     rows = {}
-    for kname in ("PH", "DTCR_UNROLL"):
+    for kname in refgpu.KERNELS:
         rk = refgpu.RefKernel(kname, sn, x.numel(), device=dev)
         for _ in range(3):
             rk(xs, y)
@@ -662,7 +662,7 @@ def run_small(dev, hbm_gbs: float) -> dict:
     if refgpu.available():
         sn, g = oracle.normalise_sos(sos)
         xsg = [(t * np.float32(g)).contiguous() for t in xs]
-        for kname in ("PH", "DTCR_UNROLL"):
+        for kname in refgpu.KERNELS:
             rk = refgpu.RefKernel(kname, sn, n, device=dev)
             ms = time_rotating(_RefAsPlan(rk), xsg, ys, 20, 200, stream)
             e = oracle.errors(ys[0].cpu().numpy(), ref)

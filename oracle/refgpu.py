@@ -1,15 +1,15 @@
 """Test and measurement infrastructure, not part of the product: the reference's own GPU kernels
-(PH_32 of include/ph_kernels.cuh and DTCR_32_UNROLL_64 of include/dtcr_kernels.cuh, from
-Haotian-RA/cuda_recursive_filtering) run on this GPU beside this library, for a kernel-to-kernel
-comparison on the same inputs.
+(PH_32, STCR_32_LOOP, STCR_32_UNROLL_64, DTCR_32_LOOP and DTCR_32_UNROLL_64 of
+include/{ph,stcr,dtcr}_kernels.cuh, from Haotian-RA/cuda_recursive_filtering) run on this GPU beside
+this library, for a kernel-to-kernel comparison on the same inputs.
 
 The reference configures a kernel at compile time (N_SECTIONS, BLOCK_SIZE, N_BLOCKS as macros) and
 prepares it on the host: setup_kernel_coefficients (ph_kernels.cuh:151-200,
 dtcr_kernels.cuh:203-289) computes float32 tables and copies them into the module's __constant__ and
 __device__ arrays. Here:
   * build_cubins() compiles the reference's headers, where they lie, into device code (one cubin per
-    configuration under oracle/_ref/; the wrapper only includes them, as src/test_performance.cu
-    does). It needs the reference's sources and runs in the build container only; the cubins travel
+    header and number of sections under oracle/_ref/, holding every kernel of the header; the wrapper
+    only includes them, as src/test_performance.cu does). It needs the reference's sources and runs in the build container only; the cubins travel
     with the repository's working tree. Device code does not depend on the host's architecture.
   * the host setup is restated below in float32 (ph_tables / dtcr_tables, following the lines cited
     there) and written into the module with the CUDA driver API (cuModuleGetGlobal, cuMemcpyHtoD);
@@ -35,10 +35,14 @@ REF_INCLUDE = "/root/reference/include"  # only where the cubins are built
 BLOCK_SIZE, N_BLOCKS = 32, 64
 CHUNK = BLOCK_SIZE * N_BLOCKS
 SECTIONS = (1, 2, 4, 8)
-# (name, header, extra macro, kernel symbol, threads per block (x, y))
+FAMILIES = {"PH": "ph_kernels.cuh", "STCR": "stcr_kernels.cuh", "DTCR": "dtcr_kernels.cuh"}
+# this library's realization name -> (the header's family, the kernel's symbol, threads per block (x, y))
 KERNELS = {
-    "PH": ("ph_kernels.cuh", None, "_Z5PH_32PKfPfPViPVfS5_i", (BLOCK_SIZE, 1)),
-    "DTCR_UNROLL": ("dtcr_kernels.cuh", "DTCR_HANDUNROLLED", "_Z17DTCR_32_UNROLL_64PKfPfPViPVfS5_i", (BLOCK_SIZE, 2)),
+    "PH": ("PH", "_Z5PH_32PKfPfPViPVfS5_i", (BLOCK_SIZE, 1)),
+    "STCR": ("STCR", "_Z12STCR_32_LOOPPKfPfPViPVfS5_i", (BLOCK_SIZE, 1)),
+    "STCR_UNROLL": ("STCR", "_Z17STCR_32_UNROLL_64PKfPfPViPVfS5_i", (BLOCK_SIZE, 1)),
+    "DTCR": ("DTCR", "_Z12DTCR_32_LOOPPKfPfPViPVfS5_i", (BLOCK_SIZE, 2)),
+    "DTCR_UNROLL": ("DTCR", "_Z17DTCR_32_UNROLL_64PKfPfPViPVfS5_i", (BLOCK_SIZE, 2)),
 }
 WRAPPER = """#include "iir_utils.hpp"
 #include "gpu_specs.hpp"
@@ -47,12 +51,12 @@ constexpr int N_TB_PER_SM = gpu_specs::compute_supply_tb_per_sm(BLOCK_SIZE, N_BL
 """
 
 
-def cubin_path(kernel: str, sections: int) -> str:
-    return os.path.join(OUT, f"{kernel.lower()}_k{sections}_{BLOCK_SIZE}x{N_BLOCKS}.cubin")
+def cubin_path(family: str, sections: int) -> str:
+    return os.path.join(OUT, f"{family.lower()}_k{sections}_{BLOCK_SIZE}x{N_BLOCKS}.cubin")
 
 
 def available() -> bool:
-    return all(os.path.exists(cubin_path(k, s)) for k in KERNELS for s in SECTIONS)
+    return all(os.path.exists(cubin_path(f, s)) for f in FAMILIES for s in SECTIONS)
 
 
 def build_cubins() -> bool:
@@ -65,23 +69,20 @@ def build_cubins() -> bool:
     os.makedirs(OUT, exist_ok=True)
 
     def one(job):
-        kernel, k = job
-        header, macro, _, _ = KERNELS[kernel]
-        out = cubin_path(kernel, k)
+        family, k = job
+        out = cubin_path(family, k)
         src = out[:-6] + ".cu"
         with open(src, "w") as f:
-            f.write(WRAPPER.format(header=header))
+            f.write(WRAPPER.format(header=FAMILIES[family]))
         cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17",
                "-I", REF_INCLUDE, f"-DN_SECTIONS={k}", f"-DBLOCK_SIZE={BLOCK_SIZE}", f"-DN_BLOCKS={N_BLOCKS}",
                "-o", out, src]
-        if macro:
-            cmd.insert(-3, f"-D{macro}")
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"reference kernel build failed ({kernel}, {k} sections):\n{r.stderr[-2000:]}")
+            raise RuntimeError(f"reference kernel build failed ({family}, {k} sections):\n{r.stderr[-2000:]}")
 
-    with cf.ThreadPoolExecutor(8) as ex:
-        list(ex.map(one, [(k, s) for k in KERNELS for s in SECTIONS]))
+    with cf.ThreadPoolExecutor(12) as ex:
+        list(ex.map(one, [(f, s) for f in FAMILIES for s in SECTIONS]))
     return True
 
 
@@ -147,15 +148,17 @@ def ph_tables(sos_norm) -> dict:
     return t
 
 
-def dtcr_tables(sos_norm) -> dict:
-    """The arrays setup_kernel_coefficients fills for DTCR (dtcr_kernels.cuh:108-289): the
-    elimination factors of every level, the decoupled first-round taps, the block-filtering
-    factors and C^(m+1)."""
+def cr_tables(sos_norm, decoupled: bool) -> dict:
+    """The arrays setup_kernel_coefficients fills for STCR (stcr_kernels.cuh:93-275) and, with the
+    decoupled first-round taps cb .. gb, for DTCR (dtcr_kernels.cuh:108-289): the elimination
+    factors of every level, the block-filtering factors and C^(m+1)."""
     L = int(np.log2(N_BLOCKS))
     cf_ = _coeffs(sos_norm)
     K = len(cf_)
-    t = {name: np.zeros(K, np.float32) for name in ("b1", "b2", "a1", "a2", "xi1", "xi2", "yi1", "yi2",
-                                                     "cb", "db", "fb", "eb", "hb", "gb")}
+    t = {name: np.zeros(K, np.float32) for name in ("b1", "b2", "a1", "a2", "xi1", "xi2", "yi1", "yi2")}
+    if decoupled:
+        for name in ("cb", "db", "fb", "eb", "hb", "gb"):
+            t[name] = np.zeros(K, np.float32)
     for name in ("e", "f", "fde", "cr_h", "cr_g", "cr_p", "cr_q", "cr_d", "cr_c"):
         t[name] = np.zeros((K, L + 1), np.float32)
     for name in ("h0", "hb2", "hb1", "he2", "he1"):
@@ -182,8 +185,9 @@ def dtcr_tables(sos_norm) -> dict:
                 p[n] = f32(f[n - 1] - f32(e[n - 1] * p[n - 1]))
         dc = [f32(f32(f[0] * b1) - f32(e[0] * b2)), f32(b1 - e[0]), f32(b2 * f[0]),
               f32(f32(b2 + f[0]) - f32(b1 * e[0])), f32(b2 - f32(e[0] * b1)), f32(-e[0] * b2)]
-        for name, v in zip(("cb", "db", "fb", "eb", "hb", "gb"), dc):
-            t[name][s] = v
+        if decoupled:
+            for name, v in zip(("cb", "db", "fb", "eb", "hb", "gb"), dc):
+                t[name][s] = v
         for name, v in (("e", e), ("f", f), ("fde", fde), ("cr_h", h), ("cr_g", g), ("cr_p", p), ("cr_q", q),
                         ("cr_d", d), ("cr_c", c)):
             t[name][s] = v
@@ -231,9 +235,9 @@ class RefKernel:
         import torch
         if n <= 0 or n % CHUNK:
             raise ValueError(f"the reference's kernels take whole chunks of {CHUNK} samples")
-        header, _, sym, block = KERNELS[kernel]
+        family, sym, block = KERNELS[kernel]
         k = np.asarray(sos_norm).reshape(-1, 6).shape[0]
-        path = cubin_path(kernel, k)
+        path = cubin_path(family, k)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         torch.zeros(1, device=device)  # the primary context is current on this thread
@@ -242,7 +246,7 @@ class RefKernel:
         _ck(cu.cuModuleLoad(ctypes.byref(self.mod), path.encode()), "cuModuleLoad")
         self.fn = ctypes.c_void_p()
         _ck(cu.cuModuleGetFunction(ctypes.byref(self.fn), self.mod, sym.encode()), "cuModuleGetFunction")
-        tables = ph_tables(sos_norm) if kernel == "PH" else dtcr_tables(sos_norm)
+        tables = ph_tables(sos_norm) if family == "PH" else cr_tables(sos_norm, decoupled=family == "DTCR")
         for name, arr in tables.items():
             dptr, size = ctypes.c_uint64(), ctypes.c_size_t()
             _ck(cu.cuModuleGetGlobal_v2(ctypes.byref(dptr), ctypes.byref(size), self.mod, name.encode()),

@@ -1,9 +1,10 @@
-"""The reference's own GPU kernels against this library on the same inputs: PH_32 and
-DTCR_32_UNROLL_64 (include/ph_kernels.cuh, include/dtcr_kernels.cuh at BLOCK_SIZE 32, N_BLOCKS 64),
+"""The reference's own GPU kernels against this library on the same inputs: PH_32, STCR_32_LOOP,
+STCR_32_UNROLL_64, DTCR_32_LOOP and DTCR_32_UNROLL_64 (include/{ph,stcr,dtcr}_kernels.cuh at
+BLOCK_SIZE 32, N_BLOCKS 64),
 compiled from the reference's sources into device code and launched under its own contract
 (oracle/refgpu.py). Both meet the reference's gate against the FP64 oracle (max|err| <= 1e-4
-max|ref|, src/test_accuracy.cu:178-188), and this library's PH / DTCR_UNROLL output agrees with the
-reference kernel's within 1e-5 of the output's peak (both are float32; each is within about 1e-6 of
+max|ref|, src/test_accuracy.cu:178-188), and this library's output of the same realization and
+geometry agrees with the reference kernel's within 1e-5 of the output's peak (both are float32; each is within about 1e-6 of
 FP64 here). Skipped where the cubins were not built (they need the reference's sources)."""
 import numpy as np
 import pytest
@@ -17,7 +18,7 @@ pytestmark = [pytest.mark.gpu,
               pytest.mark.skipif(not refgpu.available(), reason="reference kernels not built (oracle/_ref)")]
 
 
-@pytest.mark.parametrize("kernel", ("PH", "DTCR_UNROLL"))
+@pytest.mark.parametrize("kernel", tuple(refgpu.KERNELS))
 @pytest.mark.parametrize("order", (2, 4, 8, 16))
 def test_reference_kernel_agrees_with_library(kernel, order, cuda_device):
     from scipy import signal
