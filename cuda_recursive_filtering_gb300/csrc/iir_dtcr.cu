@@ -42,6 +42,19 @@ static void add(std::vector<KernelEntry>& reg) {
     reg.push_back(t);
 }
 
+// A one-tile (32-row) tail kernel for short single-section signals: more, shorter chunks, so
+// a launch ends sooner.
+template <int B, int N, int ROWS, bool UNROLL>
+static void add_tiny(std::vector<KernelEntry>& reg) {
+    using Blk = CrBlock<true, B, N, ROWS, UNROLL, true, true>;
+    const int kind = UNROLL ? IIR_KIND_DTCR_UNROLL : IIR_KIND_DTCR;
+    KernelEntry t{kind, B, N, (const void*)iir_dtcr_tail_kernel<B, N, ROWS, UNROLL>, Blk::THREADS, Blk::SMEM_BYTES,
+                  0, ROWS};
+    t.tail = 1;
+    t.tiny = 1;
+    reg.push_back(t);
+}
+
 template <int B, int N, int ROWS, bool UNROLL, int S, int D>
 __global__ void __launch_bounds__(64 + CrTwo<true, B, N, ROWS, UNROLL>::NW * 32,
                                   TwoPassGeom<ROWS, N, S, D>::min_blocks(64 + CrTwo<true, B, N, ROWS, UNROLL>::NW * 32))
@@ -84,6 +97,8 @@ static void add_geometry_set(std::vector<KernelEntry>& reg) {
 void register_dtcr(std::vector<KernelEntry>& reg) {
     add_geometry_set<32, true>(reg);
     add_geometry_set<32, false>(reg);
+    add_tiny<32, 64, 32, true>(reg);
+    add_tiny<32, 64, 32, false>(reg);
     add_geometry_set<64, true>(reg);
     add_geometry_set<64, false>(reg);
 }

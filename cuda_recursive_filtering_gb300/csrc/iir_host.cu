@@ -51,9 +51,10 @@ std::vector<KernelEntry>& registry() {
     return reg;
 }
 
-const KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline, int tail) {
+const KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline, int tail, int tiny) {
     for (const KernelEntry& e : registry())
-        if (e.kind == kind && e.B == B && e.N == N && e.order == order && e.pipeline == pipeline && e.tail == tail)
+        if (e.kind == kind && e.B == B && e.N == N && e.order == order && e.pipeline == pipeline && e.tail == tail &&
+            e.tiny == tiny)
             return &e;
     return nullptr;
 }
@@ -466,6 +467,12 @@ struct iir_plan {
     float4* d_tables_small = nullptr;
     int small_pieces = 0;
     size_t small_max_n = 0;
+    // ... and, where one is registered, a 32-row tail kernel for signals of at most tiny_max_n
+    // samples: more and shorter chunks, so that a short signal's launch ends sooner.
+    const KernelEntry* tiny = nullptr;
+    float4* d_tables_tiny = nullptr;
+    int tiny_pieces = 0;
+    size_t tiny_max_n = 0;
 };
 
 namespace {
@@ -507,6 +514,13 @@ size_t small_signal_limit(int kind, bool tail) {
     const char* v = std::getenv("IIR_GB300_SMALL_N");
     if (v) return static_cast<size_t>(std::strtoull(v, nullptr, 10));
     return (kind == IIR_KIND_PH && tail) ? ~size_t(0) : (size_t(1) << 23);
+}
+
+// Largest signal a single-section plan filters with its 32-row kernel (IIR_GB300_TINY_N; read when
+// a plan is created).
+size_t tiny_signal_limit() {
+    const char* v = std::getenv("IIR_GB300_TINY_N");
+    return v ? static_cast<size_t>(std::strtoull(v, nullptr, 10)) : (size_t(1) << 18);
 }
 
 // 64-bit words of carry slots per section (chunk slots, then one slot per group of chunks)
@@ -582,6 +596,10 @@ int plan_common_alloc(iir_plan* p, size_t max_n) {
         if (blocks_per_sm(*p->small, p->device) <= 0) return IIR_ERR_UNSUPPORTED;
         chunk = std::min(chunk, chunk_samples(p, p->small));
     }
+    if (p->tiny) {
+        if (blocks_per_sm(*p->tiny, p->device) <= 0) return IIR_ERR_UNSUPPORTED;
+        chunk = std::min(chunk, chunk_samples(p, p->tiny));
+    }
     return alloc_carry(p, (std::max<size_t>(max_n, 1) + chunk - 1) / chunk, nullptr);
 }
 
@@ -600,6 +618,7 @@ void plan_free(iir_plan* p) {
     if (p->d_carry) cudaFree(p->d_carry);
     if (p->d_tables) cudaFree(p->d_tables);
     if (p->d_tables_small) cudaFree(p->d_tables_small);
+    if (p->d_tables_tiny) cudaFree(p->d_tables_tiny);
     if (p->d_fac) cudaFree(p->d_fac);
     delete p;
 }
@@ -798,23 +817,25 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     const KernelEntry* e = nullptr;
     // The tail-aggregate kernel (iir_tail.cuh) when the cascade's state decays within half a
     // chunk, in pieces of IIR_TAIL_PIECE samples, one per warp of the block; else nullptr.
-    auto pick_tail = [&](int& pc, std::vector<float>& phi) -> const KernelEntry* {
+    auto pick_tail = [&](int& pc, std::vector<float>& phi, int tiny_kernel = 0) -> const KernelEntry* {
         if (tail_max_pieces() <= 0) return nullptr;
-        const KernelEntry* t = find_entry(kernel, B, N, 0, 0, 1);
+        const KernelEntry* t = find_entry(kernel, B, N, 0, 0, 1, tiny_kernel);
         if (!t) return nullptr;
         const int cap = std::min({tail_max_pieces(), t->threads / 32, IIR_TAIL_MAX_PIECES,
                                   t->rows * N / (2 * IIR_TAIL_PIECE)});
         pc = cap > 0 ? tail_pieces(secs.data(), n_sections, cap, phi) : 0;
         return pc > 0 ? t : nullptr;
     };
-    int pieces = 0, small_pieces = 0;
-    std::vector<float> phi, small_phi;
+    int pieces = 0, small_pieces = 0, tiny_pieces = 0;
+    std::vector<float> phi, small_phi, tiny_phi;
     const KernelEntry* small = nullptr;
+    const KernelEntry* tiny = nullptr;
     if (n_sections == 1 && pipeline_enabled()) e = find_entry(kernel, B, N, 0, 1);
     if (e) {
         // single section on the persistent schedule: a one-block-per-chunk kernel for small signals
         small = pick_tail(small_pieces, small_phi);
         if (!small) small = find_entry(kernel, B, N, 0, 0);
+        tiny = pick_tail(tiny_pieces, tiny_phi, 1);
     } else if (n_sections > 1) {
         // cascades whose state decays within a chunk: one lookback per chunk
         e = pick_tail(pieces, phi);
@@ -831,6 +852,9 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     p->small = small;
     p->small_pieces = small_pieces;
     p->small_max_n = small ? small_signal_limit(kernel, small_pieces > 0) : 0;
+    p->tiny = tiny;
+    p->tiny_pieces = tiny_pieces;
+    p->tiny_max_n = tiny ? tiny_signal_limit() : 0;
     IirParams& q = p->params;
     std::memset(&q, 0, sizeof(q));
     // lane tables of every section for kernel k (rows per chunk), then (tail schedule) the
@@ -850,9 +874,10 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
                         ph.size() * sizeof(float));
         return static_cast<int>(IIR_OK);
     };
-    std::vector<float4> tabs, tabs_small;
+    std::vector<float4> tabs, tabs_small, tabs_tiny;
     st = build_tables(e, phi, tabs);
     if (!st && small) st = build_tables(small, small_phi, tabs_small);
+    if (!st && tiny) st = build_tables(tiny, tiny_phi, tabs_tiny);
     if (st) {
         delete p;
         return st;
@@ -864,6 +889,10 @@ int iir_plan_create(iir_plan** out, const float* sos, int n_sections, int kernel
     if (!st && small) st = cuda_status(cudaMalloc(&p->d_tables_small, tabs_small.size() * sizeof(float4)));
     if (!st && small)
         st = cuda_status(cudaMemcpy(p->d_tables_small, tabs_small.data(), tabs_small.size() * sizeof(float4),
+                                    cudaMemcpyHostToDevice));
+    if (!st && tiny) st = cuda_status(cudaMalloc(&p->d_tables_tiny, tabs_tiny.size() * sizeof(float4)));
+    if (!st && tiny)
+        st = cuda_status(cudaMemcpy(p->d_tables_tiny, tabs_tiny.data(), tabs_tiny.size() * sizeof(float4),
                                     cudaMemcpyHostToDevice));
     if (st) {
         plan_free(p);
@@ -899,8 +928,9 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
     }
     // the kernel for this signal: a single-section plan's small-signal kernel up to its limit
     // (a piece that starts from a carried state always takes the persistent schedule)
-    const bool use_small = p->small && !zi && n <= p->small_max_n;
-    const KernelEntry* ent = use_small ? p->small : p->entry;
+    const bool use_tiny = p->tiny && !zi && n <= p->tiny_max_n;
+    const bool use_small = !use_tiny && p->small && !zi && n <= p->small_max_n;
+    const KernelEntry* ent = use_tiny ? p->tiny : use_small ? p->small : p->entry;
     const size_t chunk = chunk_samples(p, ent);
     const size_t nchunks = (n + chunk - 1) / chunk;
     if (nchunks > 0xffffffffull) return IIR_ERR_TOO_LARGE;
@@ -952,8 +982,8 @@ int plan_launch(iir_plan* p, const float* x, float* y, size_t n, const float* zi
         q.timeout_ns = p->timeout_ns;
         q.withhold_chunk = p->withhold;
         q.zi = ent->pipeline ? zi : nullptr;
-        q.tables = use_small ? p->d_tables_small : p->d_tables;
-        q.tail_pieces = use_small ? p->small_pieces : p->pieces;
+        q.tables = use_tiny ? p->d_tables_tiny : use_small ? p->d_tables_small : p->d_tables;
+        q.tail_pieces = use_tiny ? p->tiny_pieces : use_small ? p->small_pieces : p->pieces;
         void* args[] = {&q};
         if (ent->pipeline) {
             // persistent: at most every resident block, all co-resident (cooperative launch)

@@ -16,7 +16,8 @@ struct SectionF32 {
 };
 
 // Registered kernel for (realization, B, N, order, schedule); nullptr if none.
-const iirgb::KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline = 0, int tail = 0);
+const iirgb::KernelEntry* find_entry(int kind, int B, int N, int order, int pipeline = 0, int tail = 0,
+                                     int tiny = 0);
 // Resident blocks per SM for a registered kernel; also sets its dynamic shared memory limit.
 int blocks_per_sm(const iirgb::KernelEntry& e, int device);
 // scipy SOS rows -> b0 = a0 = 1 sections (FP64 division, float32 result) and the gain.

@@ -36,6 +36,17 @@ static void add_ph(std::vector<KernelEntry>& reg) {
     reg.push_back(t);
 }
 
+// A 32-row tail kernel for short single-section signals: more, shorter chunks (a 2^16-sample
+// signal is 32 chunks of 2048 instead of 8 of 8192), so a launch ends sooner.
+template <int B, int N, int ROWS>
+static void add_ph_tiny(std::vector<KernelEntry>& reg) {
+    KernelEntry t{IIR_KIND_PH, B, N, (const void*)iir_ph_tail_kernel<B, N, ROWS>, 32 + ROWS,
+                  BlockGeom<ROWS, N>::SMEM_BYTES, 0, ROWS};
+    t.tail = 1;
+    t.tiny = 1;
+    reg.push_back(t);
+}
+
 #ifndef IIR_TWO_STAGES
 #define IIR_TWO_STAGES 3
 #endif
@@ -75,6 +86,8 @@ void register_ph(std::vector<KernelEntry>& reg) {
     add_ph<64, 32, 128>(reg);
     add_ph<64, 64, IIR_TICKET_ROWS_N64>(reg);
     add_ph<64, 128, 64>(reg);
+    add_ph_tiny<32, 64, 32>(reg);
+    add_ph_tiny<64, 64, 32>(reg);
 }
 
 }  // namespace iirgb

@@ -30,6 +30,7 @@ struct KernelEntry {
     int pipeline = 0;  // 1: single-section persistent pipeline, launched cooperatively
     int planes = 1;    // chunk buffer layout: 1 = planes of 32-sample columns, 0 = lines (swz)
     int tail = 0;      // 1: cascade kernel on the tail-aggregate schedule (iir_tail.cuh)
+    int tiny = 0;      // 1: a 32-row tail kernel that single-section plans use for short signals
 };
 
 void register_ph(std::vector<KernelEntry>& reg);

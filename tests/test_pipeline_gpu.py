@@ -24,9 +24,11 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(autouse=True)
 def _persistent_schedule_at_every_size(monkeypatch):
-    # single-section plans take a one-block-per-chunk kernel up to 2^23 samples by default;
-    # these tests are about the persistent two-pass schedule, so it takes every size here
+    # single-section plans take one-block-per-chunk kernels up to 2^23 samples by default (a
+    # 32-row one up to 2^18); these tests are about the persistent two-pass schedule, so it takes
+    # every size here
     monkeypatch.setenv("IIR_GB300_SMALL_N", "0")
+    monkeypatch.setenv("IIR_GB300_TINY_N", "0")
 
 PIPE_KERNELS = ["PH", "STCR", "STCR_UNROLL", "DTCR", "DTCR_UNROLL"]
 PIPE_GEOMS = [(32, 32), (32, 64), (32, 128), (64, 64)]
