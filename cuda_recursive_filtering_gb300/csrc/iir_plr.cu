@@ -8,7 +8,10 @@
 //      sum_j fac_j[u] * y_lower[w/2 - K + j], fac_j = n-nacci factors (response at offset u to
 //      a unit value in history slot j; plr_kernels.cuh:564-632);
 //   3. inter-warp doubling with the same factors through shared memory (plr_kernels.cuh:634-785);
-//   4. segment chaining over the X values per thread (plr_kernels.cuh:787-811);
+//   4. segment chaining over the X values per thread (plr_kernels.cuh:787-811): here one thread
+//      chains the segments' end states with the segment transition (fac_j at the last K offsets)
+//      and every segment is then corrected at once, instead of one segment after another with two
+//      block barriers each;
 //   5. K-dimensional decoupled lookback for the chunk's incoming state and the carry correction
 //      val += sum_j fac_j[i] X_j (plr_kernels.cuh:813-899). The lookback is truncated to the m
 //      preceding chunks' aggregates when the chunk transition has decayed (||Phi^m|| <= 1e-10),
@@ -31,7 +34,8 @@ struct PlrBlock {
         float xs[KO + CHUNK];           // input of the chunk with K samples of history
         float sfac[KO][BT];             // fac_j[i] for i < BT
         float wlast[NWR][X][KO];        // last K values of each warp per segment
-        float seglast[KO];              // last K values of the previous segment
+        float seglast[X][KO];           // last K values of each segment solved from zero state
+        float segin[X][KO];             // each segment's true history (last K values of the one before)
         float part[KO];
         float Xc[KO];
         unsigned int chunk, epoch;
@@ -117,16 +121,40 @@ struct PlrBlock {
                 }
                 named_barrier_rows(NWR);
             }
-            // 4. segment chaining
+            // 4. segment chaining. Segment v (BT samples) was solved from zero history; its true
+            // last K values are L_v = local_v + Phi L_(v-1), Phi[i][j] = fac_j[BT - K + i] (the
+            // response at the segment's last K offsets to history slot j), L_(-1) = 0 (the chunk's
+            // own history enters with the carry, step 5); then segment v adds the response to
+            // L_(v-1) at every sample.
+            if constexpr (X > 1) {
+                if (rw == NWR - 1 && lane >= 32 - KO) {
 #pragma unroll
-            for (int v = 1; v < X; ++v) {
-                if (rw == NWR - 1 && lane >= 32 - KO) sm.seglast[lane - (32 - KO)] = val[v - 1];
+                    for (int v = 0; v < X; ++v) sm.seglast[v][lane - (32 - KO)] = val[v];
+                }
+                named_barrier_rows(NWR);
+                if (t < KO) {  // K threads, one component each, in lockstep within the first warp
+                    float L = sm.seglast[0][t];
+#pragma unroll
+                    for (int v = 1; v < X; ++v) {
+                        sm.segin[v][t] = L;
+                        __syncwarp(0xffffffffu >> (32 - KO));
+                        float nl = sm.seglast[v][t];
+#pragma unroll
+                        for (int j = 0; j < KO; ++j) nl = fmaf(sm.sfac[j][BT - KO + t], sm.segin[v][j], nl);
+                        __syncwarp(0xffffffffu >> (32 - KO));
+                        L = nl;
+                    }
+                    sm.part[t] = L;
+                }
                 named_barrier_rows(NWR);
 #pragma unroll
-                for (int j = 0; j < KO; ++j) val[v] = fmaf(sm.sfac[j][t], sm.seglast[j], val[v]);
-                named_barrier_rows(NWR);
+                for (int v = 1; v < X; ++v) {
+#pragma unroll
+                    for (int j = 0; j < KO; ++j) val[v] = fmaf(sm.sfac[j][t], sm.segin[v][j], val[v]);
+                }
+            } else {
+                if (rw == NWR - 1 && lane >= 32 - KO) sm.part[lane - (32 - KO)] = val[X - 1];
             }
-            if (rw == NWR - 1 && lane >= 32 - KO) sm.part[lane - (32 - KO)] = val[X - 1];
         }
         __syncthreads();  // (A) chunk aggregate in sm.part
         if (!row) {
