@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY. Nothing in the library links or calls this file; only tests/,
  * __graft_entry__.smoke() and the CPU-baseline / reference legs of bench.py load it, and only
- * as the checker (or as the timed CPU implementation of the reference's golden path).
+ * as the reference output results are compared with (or as the timed CPU implementation of the
+ * reference's golden path).
  *
  * Restated algorithms (own code, from the reference's behaviour):
  *   oracle_sosfilt_f64   — the reference's golden output: tools/ref_generate.py:89 calls

@@ -9,9 +9,10 @@ dtcr_kernels.cuh:203-289) computes float32 tables and copies them into the modul
 __device__ arrays. Here:
   * build_cubins() compiles the reference's headers, where they lie, into device code (one cubin per
     header and number of sections under oracle/_ref/, holding every kernel of the header; the wrapper
-    only includes them, as src/test_performance.cu does). It needs the reference's sources and runs in the build container only; the cubins travel
-    with the repository's working tree. Device code does not depend on the host's architecture.
-  * the host setup is restated below in float32 (ph_tables / dtcr_tables, following the lines cited
+    only includes them, as src/test_performance.cu does). It needs the reference's sources, so it
+    runs only where they are; elsewhere the cubins are used as they were built, which device code
+    allows, as it does not depend on the host's architecture.
+  * the host setup is restated below in float32 (ph_tables / cr_tables, following the lines cited
     there) and written into the module with the CUDA driver API (cuModuleGetGlobal, cuMemcpyHtoD);
   * RefKernel launches the kernel under the reference's contract (ph_kernels.cuh:16-29): a status
     buffer zeroed once, the same grid on every launch of a module, launch index 0, 1, 2, ...; so each
@@ -61,8 +62,8 @@ def available() -> bool:
 
 def build_cubins() -> bool:
     """Compiles every configuration from the reference's sources (sm_103a device code). Returns
-    False, changing nothing, where the sources or nvcc are absent (the GPU machine: it uses the cubins
-    built here)."""
+    False, changing nothing, where the sources or nvcc are absent (the cubins built earlier are
+    then used as they are)."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not (os.path.isdir(REF_INCLUDE) and os.path.exists(nvcc)):
         return False
