@@ -120,7 +120,9 @@ struct BatchBlock {
         c = __shfl_sync(FULL_MASK, c, 0);
         const bool more = c < p.nchunks;
         uint32_t lo = 0;
-        if (more) {
+        if (more && p.chunk_seg) {
+            lo = __ldg(p.chunk_seg + c);  // a bound table's precomputed map
+        } else if (more) {
             uint32_t hi = p.nsegs;  // answer in [lo, hi)
             while (hi - lo > 1) {
                 const uint32_t span = hi - lo;
@@ -756,6 +758,7 @@ struct iir_batch_bound {
     int shape = 0;
     IirBatchSegment* d_segs = nullptr;
     unsigned int* d_starts = nullptr;
+    unsigned int* d_chunk_seg = nullptr;  // each chunk's segment: no search in the launch
     IirBatchParams params{};
     unsigned int nchunks = 0;
 };
@@ -784,6 +787,10 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
         if (chunk0 > 0x7fffffffull) return IIR_ERR_TOO_LARGE;
     }
     starts[n_segs] = static_cast<unsigned int>(chunk0);
+    // each chunk's segment (the last of equal starts: empty segments have no chunks)
+    std::vector<unsigned int> cseg(std::max<size_t>(chunk0, 1), 0u);
+    for (int i = 0; i < n_segs; ++i)
+        for (unsigned int c = starts[i]; c < starts[i + 1]; ++c) cseg[c] = static_cast<unsigned int>(i);
     int st = cuda_status(cudaDeviceSynchronize());
     if (st) return st;
     if (chunk0 > b->carry_cap || group0 > b->gcap) {
@@ -796,6 +803,10 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
     h->nchunks = static_cast<unsigned int>(chunk0);
     st = cuda_status(cudaMalloc(&h->d_segs, hs.size() * sizeof(IirBatchSegment)));
     if (!st) st = cuda_status(cudaMalloc(&h->d_starts, starts.size() * sizeof(unsigned int)));
+    if (!st) st = cuda_status(cudaMalloc(&h->d_chunk_seg, cseg.size() * sizeof(unsigned int)));
+    if (!st)
+        st = cuda_status(
+            cudaMemcpy(h->d_chunk_seg, cseg.data(), cseg.size() * sizeof(unsigned int), cudaMemcpyHostToDevice));
     if (!st)
         st = cuda_status(cudaMemcpy(h->d_segs, hs.data(), hs.size() * sizeof(IirBatchSegment), cudaMemcpyHostToDevice));
     if (!st)
@@ -804,10 +815,12 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
     if (st) {
         if (h->d_segs) cudaFree(h->d_segs);
         if (h->d_starts) cudaFree(h->d_starts);
+        if (h->d_chunk_seg) cudaFree(h->d_chunk_seg);
         delete h;
         return st;
     }
     h->params = batch_params(b, k, h->d_segs, h->d_starts, static_cast<unsigned int>(n_segs), h->nchunks, -1);
+    h->params.chunk_seg = h->d_chunk_seg;
     *out = h;
     return IIR_OK;
 }
@@ -833,6 +846,7 @@ int iir_batch_unbind(iir_batch_bound* h) {
     cudaDeviceSynchronize();
     cudaFree(h->d_segs);
     cudaFree(h->d_starts);
+    cudaFree(h->d_chunk_seg);
     delete h;
     return IIR_OK;
 }

@@ -158,6 +158,7 @@ struct IirBatchSegment {
 struct IirBatchParams {
     const IirBatchSegment* segs;
     const unsigned int* chunk_start;  // [nsegs + 1], chunk_start[i] = segs[i].chunk0
+    const unsigned int* chunk_seg;    // [nchunks]: each chunk's segment (bound tables), or null: search chunk_start
     const IirBatchFilter* filters;
     const IirSection* secs;
     const float4* tables;             // [sections][IIR_BT_STRIDE], for the launch's chunk shape
