@@ -11,12 +11,13 @@
 // segment. The block that holds a segment's last sample writes zf. A chunk only ever waits for
 // a chunk drawn before it, which a running block holds, so the queue cannot deadlock.
 //
-// Each filter takes one of two schedules (chosen per filter when the chunk shape is set):
-//   * per-section lookback: each section publishes the chunk's zero-state aggregate and waits
-//     for its predecessor's (control(); two block barriers per section);
-//   * tail aggregate (iir_tail.cuh), when the filter's cascade state decays within half a chunk:
-//     the chunk's aggregate of every section comes from its last pieces, published at once; the
-//     chunk reads its predecessor's and the row warps run every section with one barrier each.
+// Two schedules:
+//   * per-section lookback (the default): each section publishes the chunk's zero-state
+//     aggregate and waits for its predecessor's (control(); two block barriers per section);
+//   * tail aggregate (iir_tail.cuh), for segments of at least IIR_GB300_BATCH_TAIL_CHUNKS chunks
+//     whose filter's cascade state decays within half a chunk: the chunk's aggregate of every
+//     section comes from its last pieces, published at once; the chunk reads its predecessor's
+//     and the row warps run every section with one barrier each.
 //
 // The chunk shape (rows x samples per row) is a run-time choice among compiled instantiations
 // (iir_batch_set_shape): long channels favour big chunks (fewer lookbacks per sample), short ones
@@ -110,6 +111,16 @@ struct BatchBlock {
         return ok;
     }
 
+    // Bulk L2 prefetch of chunk c's whole 16-byte granules (those inside its segment).
+    __device__ static void prefetch_chunk(const IirBatchParams& p, uint32_t c) {
+        const IirBatchSegment& sg = p.segs[__ldg(p.chunk_seg + c)];
+        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
+        const long long ce = cs + CHUNK < sg.n ? cs + CHUNK : sg.n;
+        const uintptr_t a = (reinterpret_cast<uintptr_t>(sg.x + cs) + 15u) & ~static_cast<uintptr_t>(15u);
+        const uintptr_t b = reinterpret_cast<uintptr_t>(sg.x + ce) & ~static_cast<uintptr_t>(15u);
+        if (b > a) prefetch_l2_bulk(reinterpret_cast<const void*>(a), static_cast<uint32_t>(b - a));
+    }
+
     // Warp 0: draws the block's next chunk from the launch's queue and finds its segment: the
     // last s with chunk_start[s] <= c (empty segments share their start with the next one, so
     // the last such index is the non-empty one). 32-way search: each round the lanes probe 32
@@ -144,18 +155,82 @@ struct BatchBlock {
         }
     }
 
-    // All threads: start copying chunk c of segment `seg` into buf (cp.async, no registers held),
-    // zero past the segment's end. Whole chunks of a 16-byte-aligned segment move as 16-byte
-    // copies, the rest sample by sample. Completion: the caller's cp_async_wait and barrier.
+    // Whole chunk of a segment that starts A floats past a 16-byte boundary (A = 1..3): granule j
+    // of the chunk (samples 4j..4j+3) is the last 4 - A floats of the aligned granule at src - A +
+    // 4j and the first A of the next one, read as two 16-byte loads (the second is the next
+    // thread's first, an L1 hit). A granule reaching past the segment (before its first sample, or
+    // past its last) is read sample by sample instead.
+    template <int A>
+    __device__ static void stage_shifted(const float* src, bool head_in, bool tail_in, float* buf, int tid) {
+        const float4* g = reinterpret_cast<const float4*>(src - A);
+        if (tid == 0) {
+            // the chunk's whole granules into L2 first (one bulk prefetch), so that the loads
+            // below, a few in flight per thread, wait for L2 rather than for memory
+            const int k0 = head_in ? 0 : 1, k1 = tail_in ? CHUNK / 4 : CHUNK / 4 - 1;  // inclusive
+            prefetch_l2_bulk(g + k0, static_cast<uint32_t>((k1 - k0 + 1) * 16));
+        }
+#pragma unroll 4
+        for (int j = tid; j < CHUNK / 4; j += THREADS) {
+            float4 v;
+            if ((j == 0 && !head_in) || (j == CHUNK / 4 - 1 && !tail_in)) {
+                v = make_float4(__ldg(src + 4 * j), __ldg(src + 4 * j + 1), __ldg(src + 4 * j + 2),
+                                __ldg(src + 4 * j + 3));
+            } else {
+                const float4 u = __ldg(g + j), w = __ldg(g + j + 1);
+                if constexpr (A == 1) v = make_float4(u.y, u.z, u.w, w.x);
+                else if constexpr (A == 2) v = make_float4(u.z, u.w, w.x, w.y);
+                else v = make_float4(u.w, w.x, w.y, w.z);
+            }
+            *reinterpret_cast<float4*>(buf + swz<N, ROWS, true>((4 * j) / N, (4 * j) % N)) = v;
+        }
+    }
+
+    // Whole chunk written to dst, B floats past a 16-byte boundary (B = 1..3): the aligned granule k
+    // of the output (chunk samples 4k - B .. 4k - B + 3) is the last B floats of the chunk's granule
+    // k - 1 and the first 4 - B of its granule k, one 16-byte store. The two end granules hold
+    // samples of the neighbouring chunks: only this chunk's samples in them are written.
+    template <int B>
+    __device__ static void store_shifted(float* dst, const float* buf, int tid) {
+        float4* g = reinterpret_cast<float4*>(dst - B);
+        const float4* s = reinterpret_cast<const float4*>(buf);
+#pragma unroll 1
+        for (int k = tid; k <= CHUNK / 4; k += THREADS) {
+            if (k == 0) {
+                for (int t = 0; t < 4 - B; ++t) dst[t] = buf[swz<N, ROWS, true>(0, t)];
+            } else if (k == CHUNK / 4) {
+                for (int t = CHUNK - B; t < CHUNK; ++t) dst[t] = buf[swz<N, ROWS, true>(t / N, t % N)];
+            } else {
+                const float4 u = s[swz<N, ROWS, true>((4 * k - 4) / N, (4 * k - 4) % N) >> 2];
+                const float4 w = s[swz<N, ROWS, true>((4 * k) / N, (4 * k) % N) >> 2];
+                if constexpr (B == 1) g[k] = make_float4(u.w, w.x, w.y, w.z);
+                else if constexpr (B == 2) g[k] = make_float4(u.z, u.w, w.x, w.y);
+                else g[k] = make_float4(u.y, u.z, u.w, w.x);
+            }
+        }
+    }
+
+    // All threads: start copying chunk c of segment `seg` into buf, zero past the segment's end.
+    // Whole chunks move as 16-byte cp.async copies (no registers held) when the chunk starts on a
+    // 16-byte boundary, as shifted 16-byte loads when it starts on another float boundary, and
+    // sample by sample otherwise (the segment's last chunk). Completion: the caller's
+    // cp_async_wait and barrier.
     __device__ static void stage(const IirBatchParams& p, uint32_t c, uint32_t seg, float* buf, int tid) {
         const IirBatchSegment& sg = p.segs[seg];
         const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
         const long long nrem = sg.n - cs;  // > 0
         const float* src = sg.x + cs;
-        if (nrem >= CHUNK && (reinterpret_cast<uintptr_t>(sg.x) & 15u) == 0) {
+        const uintptr_t mis = reinterpret_cast<uintptr_t>(src) & 15u;
+        if (nrem >= CHUNK && mis == 0) {
 #pragma unroll 4
             for (int i = tid; i < CHUNK / 4; i += THREADS)
                 cp_async16(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N), src + 4 * i);
+        } else if (nrem >= CHUNK && (mis & 3u) == 0) {
+            // granule 0 starts before the chunk: inside the segment unless this is its first chunk;
+            // the granule after the chunk ends inside the segment if 4 more samples follow
+            const bool head_in = cs > 0, tail_in = nrem >= CHUNK + 4;
+            if (mis == 4) stage_shifted<1>(src, head_in, tail_in, buf, tid);
+            else if (mis == 8) stage_shifted<2>(src, head_in, tail_in, buf, tid);
+            else stage_shifted<3>(src, head_in, tail_in, buf, tid);
         } else {
 #pragma unroll 4
             for (int i = tid; i < CHUNK; i += THREADS) {
@@ -178,7 +253,7 @@ struct BatchBlock {
 
         const bool row_warp = warp > 0;
         const int K = flt.n_sections;
-        const bool tail = flt.tail > 0;  // the filter's schedule (uniform in the block)
+        const bool tail = flt.tail > 0 && sg.tail_ok;  // the segment's schedule (uniform in the block)
         if (tail) {
             // the chunk's aggregate from its last pieces (not for the segment's last chunk)
             const bool has_succ = nrem > CHUNK;
@@ -233,6 +308,12 @@ struct BatchBlock {
             xh1 *= gain;
             named_barrier_rows(NW);  // histories read before the first pass overwrites rows (it applies the gain)
         }
+        // Control warp, idle until the row warps' first filter pass ends: with a bound table (every
+        // chunk's segment known), the chunk one grid ahead in the queue, which some block draws
+        // about one chunk's time from now, goes into L2, so that its copy-in waits for L2 rather
+        // than for memory.
+        if (!row_warp && lane == 0 && p.chunk_seg && static_cast<unsigned long long>(c) + gridDim.x < p.nchunks)
+            prefetch_chunk(p, c + gridDim.x);
         // positions of the segment's last two samples relative to this chunk
         const long long m1 = nrem - 1, m2 = nrem - 2;  // in [0, CHUNK) when inside this chunk
         float pa1 = 0.f, pa2 = 0.f, d2 = 0.f, d1 = 0.f;
@@ -319,10 +400,15 @@ struct BatchBlock {
         if (live) Ph::correct_pass(buf, r, pa1, pa2, d2, d1);
         __syncthreads();
         const long long cnt = nrem < CHUNK ? nrem : CHUNK;
-        if (cnt == CHUNK && (reinterpret_cast<uintptr_t>(sg.y) & 15u) == 0) {
+        const uintptr_t ymis = reinterpret_cast<uintptr_t>(sg.y + cs) & 15u;
+        if (cnt == CHUNK && ymis == 0) {
             float4* dst = reinterpret_cast<float4*>(sg.y + cs);
             for (int i = tid; i < CHUNK / 4; i += THREADS)
                 dst[i] = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N));
+        } else if (cnt == CHUNK && (ymis & 3u) == 0) {
+            if (ymis == 4) store_shifted<1>(sg.y + cs, buf, tid);
+            else if (ymis == 8) store_shifted<2>(sg.y + cs, buf, tid);
+            else store_shifted<3>(sg.y + cs, buf, tid);
         } else {
             for (int i = tid; i < cnt; i += THREADS) sg.y[cs + i] = buf[swz<N, ROWS, true>(i / N, i % N)];
         }
@@ -510,6 +596,19 @@ bool batch_tail_enabled() {
     if (std::getenv("IIR_GB300_FULL_LOOKBACK")) return false;
     const char* e = std::getenv("IIR_GB300_TAIL");
     return !(e && std::atoi(e) == 0);
+}
+
+// Least number of chunks for a segment to take its filter's tail-aggregate schedule
+// (IIR_GB300_BATCH_TAIL_CHUNKS; by default none does). In the persistent batch kernel the
+// per-section lookback is the faster schedule at every segment length measured on GB300 (a
+// single 2^27-sample segment of butter(16, 0.1): 201 against 189 GS/s; the mixed 4096-channel
+// workload: 299 against 280): the other resident blocks fill the lookback waits, while the tail
+// pieces add up to half a chunk of filtering to every chunk.
+size_t batch_tail_min_chunks() {
+    const char* e = std::getenv("IIR_GB300_BATCH_TAIL_CHUNKS");
+    if (!e) return ~static_cast<size_t>(0);
+    const long long v = std::atoll(e);
+    return v > 0 ? static_cast<size_t>(v) : 1;
 }
 
 // Builds shape k's lane tables and filter records (once) and its occupancy.
@@ -732,10 +831,12 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
     IirBatchSegment* hs = reinterpret_cast<IirBatchSegment*>(b->h_stage[turn]);
     unsigned int* hstart = reinterpret_cast<unsigned int*>(b->h_stage[turn] + n_segs * sizeof(IirBatchSegment));
     unsigned int chunk0 = 0, group0 = 0;
+    const size_t tail_min = batch_tail_min_chunks();
     for (int i = 0; i < n_segs; ++i) {
         const iir_segment& s = segs[i];
         const unsigned int ch = static_cast<unsigned int>(seg_chunks(s.n, k));
-        hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, chunk0, group0, s.filter, 0};
+        hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, chunk0, group0, s.filter,
+                                ch >= tail_min ? 1 : 0};
         hstart[i] = chunk0;
         chunk0 += ch;
         group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;
@@ -770,6 +871,7 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
     std::vector<IirBatchSegment> hs(static_cast<size_t>(std::max(n_segs, 1)));
     std::vector<unsigned int> starts(static_cast<size_t>(n_segs) + 1);
     size_t chunk0 = 0, group0 = 0;
+    const size_t tail_min = batch_tail_min_chunks();
     for (int i = 0; i < n_segs; ++i) {
         const iir_segment& s = segs[i];
         if (s.filter < 0 || s.filter >= b->n_filters) return IIR_ERR_INVALID_ARGUMENT;
@@ -780,7 +882,7 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
         if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
         const size_t ch = seg_chunks(s.n, k);
         hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, static_cast<unsigned int>(chunk0),
-                                static_cast<unsigned int>(group0), s.filter, 0};
+                                static_cast<unsigned int>(group0), s.filter, ch >= tail_min ? 1 : 0};
         starts[i] = static_cast<unsigned int>(chunk0);
         chunk0 += ch;
         group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;

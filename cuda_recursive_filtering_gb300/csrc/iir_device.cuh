@@ -92,6 +92,11 @@ __device__ __forceinline__ void cp_async4(void* dst_smem, const void* src, int b
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
 }
+// Bulk prefetch of [src, src + bytes) into L2 (one instruction, no completion to wait for):
+// src 16-byte aligned, bytes a multiple of 16, the range inside the source buffer.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }

@@ -152,7 +152,7 @@ struct IirBatchSegment {
     unsigned int chunk0;    // first chunk of the segment in the launch's chunk space
     unsigned int group0;    // first group slot of the segment
     int filter;
-    int pad;
+    int tail_ok;            // long enough for its filter's tail-aggregate schedule (host's choice)
 };
 
 struct IirBatchParams {

@@ -180,7 +180,8 @@ int iir_plan_destroy(iir_plan* plan);
  * zi / zf are device arrays of 2 + 2 * n_sections floats: x[-2], x[-1] (raw input before the
  * segment), then for each section its output history y[-2], y[-1] (the filter domain after
  * b0 / a0 normalisation, the gain applied to the input). zi = NULL starts at rest; zf = NULL
- * skips the final state; zi and zf must not overlap. A segment with n = 0 writes nothing. */
+ * skips the final state; zi and zf must not overlap, and no segment's y may overlap any
+ * segment's x. A segment with n = 0 writes nothing. */
 typedef struct {
     const float* x;
     float* y;
@@ -197,9 +198,10 @@ typedef struct iir_batch iir_batch;
 int iir_batch_create(iir_batch** batch, const float* sos, const int* n_sections, int n_filters,
                      size_t max_segments, size_t max_chunks);
 /* Filters every segment in one launch on `stream`: a persistent grid draws the segments' chunks
- * from one work queue (PH solve; the decoupled lookback restricted to each segment; filters whose
- * state decays within half a chunk publish one aggregate per chunk from its tail, the others one
- * per section). Stream-ordered; launches of one batch plan must be ordered on one stream. */
+ * from one work queue (PH solve; the decoupled lookback restricted to each segment, one carry
+ * per section; with IIR_GB300_BATCH_TAIL_CHUNKS=n, segments of n chunks or more whose filter's
+ * state decays within half a chunk publish one aggregate per chunk from its tail instead).
+ * Stream-ordered; launches of one batch plan must be ordered on one stream. */
 int iir_batch_execute(iir_batch* batch, const iir_segment* segs, int n_segs, void* stream);
 int iir_batch_check(iir_batch* batch, void* stream);
 /* A fixed segment table uploaded once (synchronously) for repeated launches: each

@@ -202,10 +202,24 @@ def _mixed_filters():
     return _filters() + [(2, res), (16, np.vstack([signal.butter(14, 0.6, output="sos"), res]))]
 
 
+SCHEDULES = ["per_section", "tail"]
+
+
+def _schedule(monkeypatch, schedule):
+    """The batch's schedule for later launches: the per-section lookback (default) or, for every
+    segment whose filter's state decays within half a chunk, the tail aggregate."""
+    if schedule == "tail":
+        monkeypatch.setenv("IIR_GB300_BATCH_TAIL_CHUNKS", "1")
+    else:
+        monkeypatch.delenv("IIR_GB300_BATCH_TAIL_CHUNKS", raising=False)
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("shape", [(128, 64), (128, 32), (128, 16), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
-def test_every_chunk_shape(shape, cuda_device):
+def test_every_chunk_shape(shape, schedule, monkeypatch, cuda_device):
     """Every compiled chunk shape of the persistent batch kernel, channels of many lengths around
-    the chunk size with filters on both schedules, two launches in a row (new epoch, same slots)."""
+    the chunk size, with both schedules, two launches in a row (new epoch, same slots)."""
+    _schedule(monkeypatch, schedule)
     filters = _mixed_filters()
     batch = Batch([s for _, s in filters])
     batch.set_shape(*shape)
@@ -230,10 +244,13 @@ def test_every_chunk_shape(shape, cuda_device):
             _check(yt.cpu().numpy(), x, filters[f][1], filters[f][0], (shape, launch, i, x.size, f))
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
 @pytest.mark.parametrize("shape", [(128, 64), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
-def test_streamed_state_both_schedules(shape, cuda_device):
-    """A stream in random pieces with its state carried on the device, for a filter on the tail
-    schedule and one on the per-section lookback, at the largest and smallest chunk shapes."""
+def test_streamed_state_both_schedules(shape, schedule, monkeypatch, cuda_device):
+    """A stream in random pieces with its state carried on the device, with both schedules, for a
+    filter whose state decays within half a chunk and one whose state does not (it keeps the
+    per-section lookback either way), at the largest and smallest chunk shapes."""
+    _schedule(monkeypatch, schedule)
     filters = _mixed_filters()
     batch = Batch([s for _, s in filters])
     batch.set_shape(*shape)
@@ -255,16 +272,17 @@ def test_streamed_state_both_schedules(shape, cuda_device):
 
 
 def test_tail_and_per_section_schedules_agree(monkeypatch, cuda_device):
-    """The same channels with the tail-aggregate schedule and with the per-section lookback
-    everywhere (IIR_GB300_TAIL=0, read when a shape is prepared): both meet the gate and agree to
-    1e-5 of the signal's peak."""
+    """The same channels with the tail-aggregate schedule (IIR_GB300_BATCH_TAIL_CHUNKS=1) and with
+    the per-section lookback everywhere (the default, and IIR_GB300_TAIL=0, read when a shape is
+    prepared): all meet the gate and agree to 1e-5 of the signal's peak."""
     filters = _mixed_filters()
     rng = np.random.default_rng(8)
     lengths = [int(v) for v in rng.integers(1, 200_000, 30)]
     xs = [rng.uniform(-1, 1, n).astype(np.float32) for n in lengths]
     outs = []
-    for tail in (True, False):
-        if not tail:
+    for mode in ("tail", "default", "tail_off"):
+        _schedule(monkeypatch, "tail" if mode != "default" else "per_section")
+        if mode == "tail_off":
             monkeypatch.setenv("IIR_GB300_TAIL", "0")
         batch = Batch([s for _, s in filters])
         ys = [torch.empty(x.size, device="cuda") for x in xs]
@@ -275,8 +293,10 @@ def test_tail_and_per_section_schedules_agree(monkeypatch, cuda_device):
         order, sos = filters[i % len(filters)]
         _, ref = oracle.reference_golden(sos, x)
         scale = float(np.max(np.abs(ref))) or 1.0
-        assert np.max(np.abs(outs[0][i] - outs[1][i])) <= 1e-5 * scale, i
+        for k in (1, 2):
+            assert np.max(np.abs(outs[0][i] - outs[k][i])) <= 1e-5 * scale, (i, k)
         _check(outs[0][i], x, sos, order, ("tail", i))
+        _check(outs[1][i], x, sos, order, ("per-section", i))
 
 
 def test_tune_batch_picks_a_shape_and_filters_correctly(cuda_device):
@@ -302,3 +322,42 @@ def test_tune_batch_picks_a_shape_and_filters_correctly(cuda_device):
     for i in rng.choice(lengths.size, 12, replace=False):
         f = int(flt[i])
         _check(yh[off[i]:off[i + 1]], x[off[i]:off[i + 1]].cpu().numpy(), filters[f][1], filters[f][0], ("tuned", i))
+
+
+@pytest.mark.parametrize("shape", [(128, 64), (128, 32), (128, 16), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_segments_at_every_float_offset(shape, cuda_device):
+    """Segments packed into one input and one output buffer at every offset modulo 16 bytes, the
+    input and output offsets independent, with lengths at and around whole chunks (whole chunks of
+    a segment that is not 16-byte aligned move as shifted 16-byte loads and stores). Every segment
+    meets the gate, and the output samples between segments keep their sentinel."""
+    filters = _mixed_filters()
+    batch = Batch([s for _, s in filters])
+    batch.set_shape(*shape)
+    chunk = batch.shape()["chunk"]
+    rng = np.random.default_rng(31 + shape[1])
+    lengths = [chunk, chunk + 1, chunk + 3, chunk + 4, chunk + 5, 2 * chunk, 2 * chunk + 2, 3 * chunk + 3,
+               5 * chunk + 1, chunk - 1, 7, 4 * chunk + 4]
+    lengths = [n for n in lengths for _ in range(2)]
+    xo, yo, px, py = [], [], 0, 0
+    for i, n in enumerate(lengths):
+        px += i % 4          # input offsets cycle through every residue mod 4 floats
+        py += int(rng.integers(0, 6))
+        xo.append(px)
+        yo.append(py)
+        px += n
+        py += n
+    x = rng.uniform(-1, 1, px + 8).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.full((py + 8,), float("nan"), device="cuda")
+    segs = [(xt[a:a + n], yt[b:b + n], i % len(filters)) for i, (a, b, n) in enumerate(zip(xo, yo, lengths))]
+    assert {t[0].data_ptr() % 16 for t in segs} == {0, 4, 8, 12}
+    assert len({t[1].data_ptr() % 16 for t in segs}) > 1
+    batch(segs)
+    batch.check()
+    yh = yt.cpu().numpy()
+    covered = np.zeros(yh.size, bool)
+    for i, (a, b, n) in enumerate(zip(xo, yo, lengths)):
+        f = i % len(filters)
+        _check(yh[b:b + n], x[a:a + n], filters[f][1], filters[f][0], (shape, i, n, a % 4, b % 4))
+        covered[b:b + n] = True
+    assert np.isnan(yh[~covered]).all()
