@@ -155,33 +155,16 @@ struct BatchBlock {
         }
     }
 
-    // Whole chunk of a segment that starts A floats past a 16-byte boundary (A = 1..3): granule j
-    // of the chunk (samples 4j..4j+3) is the last 4 - A floats of the aligned granule at src - A +
-    // 4j and the first A of the next one, read as two 16-byte loads (the second is the next
-    // thread's first, an L1 hit). A granule reaching past the segment (before its first sample, or
-    // past its last) is read sample by sample instead.
-    template <int A>
-    __device__ static void stage_shifted(const float* src, bool head_in, bool tail_in, float* buf, int tid) {
-        const float4* g = reinterpret_cast<const float4*>(src - A);
-        if (tid == 0) {
-            // the chunk's whole granules into L2 first (one bulk prefetch), so that the loads
-            // below, a few in flight per thread, wait for L2 rather than for memory
-            const int k0 = head_in ? 0 : 1, k1 = tail_in ? CHUNK / 4 : CHUNK / 4 - 1;  // inclusive
-            prefetch_l2_bulk(g + k0, static_cast<uint32_t>((k1 - k0 + 1) * 16));
-        }
+    // Whole chunk of a segment that does not start on a 16-byte boundary: granule j of the chunk
+    // (samples 4j..4j+3, 16-byte aligned in shared memory) as two 8-byte or four 4-byte cp.async
+    // copies, as the source's alignment allows. Every copy stays within the chunk.
+    template <bool EIGHT>
+    __device__ static void stage_unaligned(const float* src, float* buf, int tid) {
 #pragma unroll 4
         for (int j = tid; j < CHUNK / 4; j += THREADS) {
-            float4 v;
-            if ((j == 0 && !head_in) || (j == CHUNK / 4 - 1 && !tail_in)) {
-                v = make_float4(__ldg(src + 4 * j), __ldg(src + 4 * j + 1), __ldg(src + 4 * j + 2),
-                                __ldg(src + 4 * j + 3));
-            } else {
-                const float4 u = __ldg(g + j), w = __ldg(g + j + 1);
-                if constexpr (A == 1) v = make_float4(u.y, u.z, u.w, w.x);
-                else if constexpr (A == 2) v = make_float4(u.z, u.w, w.x, w.y);
-                else v = make_float4(u.w, w.x, w.y, w.z);
-            }
-            *reinterpret_cast<float4*>(buf + swz<N, ROWS, true>((4 * j) / N, (4 * j) % N)) = v;
+            float* dst = buf + swz<N, ROWS, true>((4 * j) / N, (4 * j) % N);
+            if constexpr (EIGHT) cp_async16_from8(dst, src + 4 * j);
+            else cp_async16_from4(dst, src + 4 * j);
         }
     }
 
@@ -209,11 +192,10 @@ struct BatchBlock {
         }
     }
 
-    // All threads: start copying chunk c of segment `seg` into buf, zero past the segment's end.
-    // Whole chunks move as 16-byte cp.async copies (no registers held) when the chunk starts on a
-    // 16-byte boundary, as shifted 16-byte loads when it starts on another float boundary, and
-    // sample by sample otherwise (the segment's last chunk). Completion: the caller's
-    // cp_async_wait and barrier.
+    // All threads: start copying chunk c of segment `seg` into buf (cp.async, no registers held),
+    // zero past the segment's end. Whole chunks move as 16-byte copies when the chunk starts on a
+    // 16-byte boundary, else as 8- or 4-byte copies per 16-byte granule; the segment's last chunk
+    // moves sample by sample. Completion: the caller's cp_async_wait and barrier.
     __device__ static void stage(const IirBatchParams& p, uint32_t c, uint32_t seg, float* buf, int tid) {
         const IirBatchSegment& sg = p.segs[seg];
         const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
@@ -225,12 +207,8 @@ struct BatchBlock {
             for (int i = tid; i < CHUNK / 4; i += THREADS)
                 cp_async16(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N), src + 4 * i);
         } else if (nrem >= CHUNK && (mis & 3u) == 0) {
-            // granule 0 starts before the chunk: inside the segment unless this is its first chunk;
-            // the granule after the chunk ends inside the segment if 4 more samples follow
-            const bool head_in = cs > 0, tail_in = nrem >= CHUNK + 4;
-            if (mis == 4) stage_shifted<1>(src, head_in, tail_in, buf, tid);
-            else if (mis == 8) stage_shifted<2>(src, head_in, tail_in, buf, tid);
-            else stage_shifted<3>(src, head_in, tail_in, buf, tid);
+            if (mis == 8) stage_unaligned<true>(src, buf, tid);
+            else stage_unaligned<false>(src, buf, tid);
         } else {
 #pragma unroll 4
             for (int i = tid; i < CHUNK; i += THREADS) {

@@ -92,6 +92,22 @@ __device__ __forceinline__ void cp_async4(void* dst_smem, const void* src, int b
     const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
 }
+// Four floats (16 bytes) to a 16-byte-aligned destination from a source aligned to 8 bytes
+// (two 8-byte copies) or only to 4 (four 4-byte copies).
+__device__ __forceinline__ void cp_async16_from8(void* dst_smem, const void* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+    asm volatile(
+        "cp.async.ca.shared.global [%0], [%1], 8;\n\t"
+        "cp.async.ca.shared.global [%0+8], [%1+8], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16_from4(void* dst_smem, const void* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst_smem));
+    asm volatile(
+        "cp.async.ca.shared.global [%0], [%1], 4;\n\t"
+        "cp.async.ca.shared.global [%0+4], [%1+4], 4;\n\t"
+        "cp.async.ca.shared.global [%0+8], [%1+8], 4;\n\t"
+        "cp.async.ca.shared.global [%0+12], [%1+12], 4;" ::"r"(d), "l"(src) : "memory");
+}
 // Bulk prefetch of [src, src + bytes) into L2 (one instruction, no completion to wait for):
 // src 16-byte aligned, bytes a multiple of 16, the range inside the source buffer.
 __device__ __forceinline__ void prefetch_l2_bulk(const void* src, uint32_t bytes) {
