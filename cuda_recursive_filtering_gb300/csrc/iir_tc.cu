@@ -257,6 +257,26 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // barrier of one compute group (named barrier 1: front, 2: back)
 __device__ __forceinline__ void bar_group(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(TC_CT) : "memory"); }
 
+// TF32 hi / lo split of 16 samples of the staged tile xt (half `half` of k-block kb of this
+// thread's chunk row r, 128-byte swizzled rows of 32 samples) into the x operand columns of TMEM:
+// hi at xa + 16 half, lo at xa + 64 + 16 half (xa: the k-block's first column, this warp's lanes).
+__device__ __forceinline__ void tc_split16(const float* xt, int kb, int half, int r, uint32_t xa) {
+    const float4* row = reinterpret_cast<const float4*>(xt + kb * TC_KB + r * 32);
+    float hi[16], lo[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const float4 v = row[(4 * half + c) ^ (r & 7)];
+        const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            hi[4 * c + j] = tf32_hi(e[j]);
+            lo[4 * c + j] = tf32_hi(e[j] - hi[4 * c + j]);
+        }
+    }
+    tmem_st16(xa + 16 * half, hi);
+    tmem_st16(xa + 64 + 16 * half, lo);
+}
+
 // Optional timeline (compiled in with -DIIR_PROFILE): per block, per tile iteration k < 16,
 // 16 SM-clock stamps.
 #ifdef IIR_PROFILE
@@ -406,7 +426,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         mbar_init(&aux->mb_tma[1], 1);
         for (int b = 0; b < 2; ++b) {
             mbar_init(&aux->mb_g1[b], 1);  // per x buffer: tile k uses buffer k & 1
-            mbar_init(&aux->mb_split[b], 1);
+            mbar_init(&aux->mb_split[b], 2);  // one arrival per compute group (their halves of the split)
         }
         mbar_init(&aux->mb_g2, 1);
         mbar_init(&aux->mb_sready, 1);
@@ -429,6 +449,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     unsigned long long* gslots = p.carry + static_cast<size_t>(p.carry_cap) * 2 * KD;
     volatile int* vbail = &aux->bail;
     auto tile_of = [&](uint32_t kk) { return blockIdx.x + kk * G; };
+    // a whole tile of the signal, staged by TMA (else the front group gathers it)
+    auto bulk = [&](uint32_t kk) {
+        return p.use_tma && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
+    };
+    // The compute groups split a TMA-staged tile in halves (front: k-block 0, back: k-block 1) and
+    // arrive on mb_split once each; a gathered tile, and every tile of the BF16 forms, is split
+    // whole by the front group, which then arrives for both. With 16 states the back group's
+    // rescan takes twice the steps and the front's split stays whole, which balances the groups
+    // better (order 8: 334 -> 358 GS/s shared; order 16: 275 shared).
+    auto shared_split = [&](uint32_t kk) { return BF == 0 && KD <= 8 && bulk(kk); };
 
     if (warp < TC_LBW) {
         // ================= lookback warps: tiles k = warp, warp + TC_LBW, ... =================
@@ -484,8 +514,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         // unobserved: split and GEMM 1 barriers are per x buffer (tile k + 2 is staged only after
         // GEMM 1 of tile k completed), sready(k + 1) and accfree(k + 1) need GEMM 2 of tile k,
         // which is issued only after accfree(k - 1) was observed.
+        // It also issues the x tiles' TMA loads: tiles 0 and 1 at once, tile k + 2 into the buffer of
+        // tile k once both groups have split tile k (seen as its split barrier completing), so at
+        // most one load per buffer is in flight.
         if (lane == 0) {
             uint32_t k1 = 0, k2 = 0, piece = 0, n_free = 0;
+            uint32_t tma_n[2] = {0u, 0u};  // loads issued per buffer
+            auto issue_tma = [&](uint32_t kk) {
+                const int sb = kk & 1;
+                float* dst = xs + sb * 2 * TC_KB;
+                mbar_arrive_expect_tx(&aux->mb_tma[sb], 2u * TC_KB * 4u);
+                tma_load_2d(dst, &p.tmap_x, 0, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[sb]);
+                tma_load_2d(dst + TC_KB, &p.tmap_x, 32, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[sb]);
+                ++tma_n[sb];
+            };
+            for (uint32_t kk = 0; kk < 2 && kk < nk; ++kk)
+                if (bulk(kk)) issue_tma(kk);
             bool got_split = false;
             uint64_t t_last = globaltimer_ns();
             uint32_t spins = 0;
@@ -514,7 +558,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                     ++k2;
                     progress = true;
                 } else if (k1 < nk && (k1 < TC_NACC || n_free + TC_NACC > k1)) {  // accumulator k1 % TC_NACC is free
-                    if (!got_split) got_split = mbar_try_wait(&aux->mb_split[k1 & 1], (k1 >> 1) & 1u);
+                    if (!got_split) {
+                        got_split = mbar_try_wait(&aux->mb_split[k1 & 1], (k1 >> 1) & 1u);
+                        if (got_split && k1 + 2 < nk && bulk(k1 + 2)) issue_tma(k1 + 2);  // buffer k1 & 1 read out
+                    }
                     if (got_split) {
                         if (piece == 0) tc_fence_after();
                         const uint32_t xa = tmem + static_cast<uint32_t>(TC_XCOL + (k1 & 1) * 128);  // x hi; lo at + 64
@@ -565,6 +612,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                     }
                 }
             }
+            // loads still in flight (a stopped launch) land before the block leaves: the last load
+            // of each buffer completes its phase (tma_n - 1), and every earlier one had landed
+            // before the next was issued
+            for (int sb = 0; sb < 2; ++sb)
+                if (tma_n[sb] > 0) wait_mbar_bounded(&aux->mb_tma[sb], (tma_n[sb] - 1) & 1u, p.timeout_ns);
         }
         __syncwarp();
     } else if (warp < TC_CW0 + TC_CW) {
@@ -584,19 +636,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         float* V0 = U + TC_NB * TC_UP;                             // [groups][16] x 2 combine ping-pong
         float* V1 = V0 + Scan::GROUPS * TC_DMAX;
         float* SB = V1 + Scan::GROUPS * TC_DMAX;                   // [groups][16] scan state broadcast
-        uint32_t tma_par[2] = {0u, 0u}, tma_real[2] = {0u, 0u}, g1_par = 0;
-
-        auto bulk = [&](uint32_t kk) {
-            return p.use_tma && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
-        };
-        auto issue_tma = [&](uint32_t kk) {  // by ct == 0
-            const int s = kk & 1;
-            float* dst = xs + s * 2 * TC_KB;
-            mbar_arrive_expect_tx(&aux->mb_tma[s], 2u * TC_KB * 4u);
-            tma_load_2d(dst, &p.tmap_x, 0, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[s]);
-            tma_load_2d(dst + TC_KB, &p.tmap_x, 32, static_cast<int>(tile_of(kk) * TC_NB), &aux->mb_tma[s]);
-            ++tma_real[s];
-        };
+        uint32_t tma_par[2] = {0u, 0u}, g1_par = 0;
         // one recurrence step of the half-warp's state, Phi S + Z_j + Phix xh_j; the state goes
         // through the group's 16-float buffer sb (one store, four broadcast vector loads)
         auto step = [&](float S, int j, const float* xhj, float* sb) {
@@ -662,36 +702,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 aux->xh[kk % TC_NXH][ct][1] = x1;
             }
             {  // (the split only reads the staged tile, so it needs no barrier after the capture)
-                // this thread's chunk row (TMEM lane 32 q + lane), k-block hh: 32 samples from the
-                // swizzled tile, split hi / lo, stored to the x operand columns of buffer kk & 1
+                // this thread's chunk row (TMEM lane 32 q + lane): 32 samples from the swizzled tile,
+                // split hi / lo, stored to the x operand columns of buffer kk & 1 -- k-block hh (both
+                // halves) when this group splits the tile whole, else half hh of k-block 0 (the back
+                // group splits k-block 1)
                 const int r = 32 * q + lane;
-                const float4* row = reinterpret_cast<const float4*>(xt + hh * TC_KB + r * 32);
-                const uint32_t xa = tmem + (static_cast<uint32_t>(32 * q) << 16) +
-                                    static_cast<uint32_t>(TC_XCOL + (kk & 1) * 128 + 32 * hh);
+                const uint32_t xq = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(TC_XCOL + (kk & 1) * 128);
                 __syncwarp();
                 if constexpr (BF == 0) {
-#pragma unroll
-                    for (int half = 0; half < 2; ++half) {
-                        float hi[16], lo[16];
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const float4 v = row[(4 * half + c) ^ (r & 7)];
-                            hi[4 * c] = tf32_hi(v.x);
-                            hi[4 * c + 1] = tf32_hi(v.y);
-                            hi[4 * c + 2] = tf32_hi(v.z);
-                            hi[4 * c + 3] = tf32_hi(v.w);
-                            lo[4 * c] = tf32_hi(v.x - hi[4 * c]);
-                            lo[4 * c + 1] = tf32_hi(v.y - hi[4 * c + 1]);
-                            lo[4 * c + 2] = tf32_hi(v.z - hi[4 * c + 2]);
-                            lo[4 * c + 3] = tf32_hi(v.w - hi[4 * c + 3]);
-                        }
-                        tmem_st16(xa + 16 * half, hi);
-                        tmem_st16(xa + 64 + 16 * half, lo);
+                    if (shared_split(kk)) {
+                        tc_split16(xt, 0, hh, r, xq);
+                    } else {
+                        tc_split16(xt, hh, 0, r, xq + 32 * hh);
+                        tc_split16(xt, hh, 1, r, xq + 32 * hh);
                     }
                 } else {
                     // bf16 parts of the 32 samples, two per column: part a of k-block hh at columns
-                    // 32 a + 16 hh of the buffer (xa already holds + 32 hh: move it back to the buffer)
-                    const uint32_t xb = xa - static_cast<uint32_t>(32 * hh) + static_cast<uint32_t>(16 * hh);
+                    // 32 a + 16 hh of the buffer
+                    const float4* row = reinterpret_cast<const float4*>(xt + hh * TC_KB + r * 32);
+                    const uint32_t xb = xq + static_cast<uint32_t>(16 * hh);
 #pragma unroll
                     for (int half = 0; half < 2; ++half) {
                         uint32_t w[TcBf16<BF>::PARTS][8];
@@ -720,14 +749,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             fence_proxy_async_smem();  // the tile's stage is refilled by TMA next
             tc_fence_before();
             const bool stop = bar_group_any(1, *vbail);
-            if (!stop && ct == 0) mbar_arrive(&aux->mb_split[kk & 1]);
+            if (!stop && ct == 0) {
+                mbar_arrive(&aux->mb_split[kk & 1]);
+                if (!shared_split(kk)) mbar_arrive(&aux->mb_split[kk & 1]);  // the back group's share too
+            }
             return stop;
         };
 
-        if (ct == 0) {
-            for (uint32_t kk = 0; kk < 2 && kk < nk; ++kk)
-                if (bulk(kk)) issue_tma(kk);
-        }
         // the two input samples before tile kk (zero before the signal); loaded one iteration
         // ahead so the load's latency is not on the staging path
         auto hist = [&](uint32_t kk, float& h2v, float& h1v) {
@@ -738,7 +766,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         float hx2 = 0.f, hx1 = 0.f;
         if (nk > 0) hist(0, hx2, hx1);
         bool stop = nk > 0 ? stage_tile(0, hx2, hx1) : false;
-        if (ct == 0 && 2 < nk && bulk(2) && !stop) issue_tma(2);  // stage 0 was read out
         if (nk > 1) hist(1, hx2, hx1);
         for (uint32_t k = 0; k < nk && !stop; ++k) {
             if (ct == 0) TC_STAMP(k, 0);
@@ -746,7 +773,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             // completion this group saw), so GEMM 1 of tile k runs meanwhile ----
             if (k + 1 < nk) {
                 if (stage_tile(k + 1, hx2, hx1)) break;
-                if (ct == 0 && k + 3 < nk && bulk(k + 3)) issue_tma(k + 3);  // stage (k+1) & 1 is free
                 if (k + 2 < nk) hist(k + 2, hx2, hx1);
             }
             if (ct == 0) TC_STAMP(k, 7);
@@ -806,11 +832,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             }
             stop = bar_group_any(1, *vbail);
         }
-        if (ct == 0) {
-            for (int s = 0; s < 2; ++s)
-                while (tma_par[s] < tma_real[s] && wait_mbar_bounded(&aux->mb_tma[s], tma_par[s] & 1u, p.timeout_ns))
-                    ++tma_par[s];
-        }
         __syncthreads();
         if (ct == 0)  // GEMM 1 batches still in flight end before TMEM is freed
             while (g1_par < aux->g1_issued &&
@@ -864,6 +885,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 if (e + 3 < KD) s3 = fmaf(mm.w, vv.w, s3);
             }
             return (s0 + s1) + (s2 + s3);
+        };
+        // The back group's half of a TMA-staged tile's split (k-block 1; the front group splits
+        // k-block 0): once the tile has landed and GEMM 1 of tile kk - 2 has read the TMEM x buffer
+        // that this tile takes over. Returns the group's stop decision.
+        uint32_t tma_par_b[2] = {0u, 0u};
+        auto split_half = [&](uint32_t kk) {
+            if (!shared_split(kk)) return false;  // the front group splits this tile whole
+            bool ok = true;
+            if (kk >= 2) ok = tc_wait(&aux->mb_g1[(kk - 2) & 1], ((kk - 2) >> 1) & 1u, wait_lim, &aux->bail);
+            if (ok) {
+                ok = tc_wait(&aux->mb_tma[kk & 1], tma_par_b[kk & 1] & 1u, p.timeout_ns, &aux->bail);
+                if (ok) ++tma_par_b[kk & 1];
+            }
+            if (!ok) {
+                tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
+            } else {
+                tc_fence_after();
+                const float* xt = xs + (kk & 1) * 2 * TC_KB;
+                const uint32_t xq = tmem + (static_cast<uint32_t>(32 * q) << 16) +
+                                    static_cast<uint32_t>(TC_XCOL + (kk & 1) * 128 + 32);
+                __syncwarp();
+                tc_split16(xt, 1, hh, 32 * q + lane, xq);
+                tmem_wait_st();
+            }
+            fence_proxy_async_smem();
+            tc_fence_before();
+            const bool st = bar_group_any(2, *vbail);
+            if (!st && ct == 0) mbar_arrive(&aux->mb_split[kk & 1]);
+            return st;
         };
         float* vx = VX + grp * TC_DMAX;                  // the group's state buffer
         float4* patch = reinterpret_cast<float4*>(VX + Scan::GROUPS * TC_DMAX) + cw * 64;  // [32 rows][2 float4]
@@ -973,21 +1023,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         };
 
         bool stop = false;
-        if (nk > 0) {
+        for (uint32_t kk = 0; kk < 3 && kk < nk && !stop; ++kk) stop = split_half(kk);
+        if (nk > 0 && !stop) {
             prepare(0);
             stop = bar_group_any(2, *vbail) || rescan(0);
         }
         for (uint32_t k = 0; k < nk && !stop; ++k) {
-            if (k + 1 < nk) prepare(k + 1);  // overlaps GEMM 2 of tile k
-            epilogue(k);
-            // (also: rows of tile k+1 are in U, and GEMM 2 of tile k has read the state operand)
-            stop = bar_group_any(2, *vbail);
-            if (stop) break;
-            if (ct == 0) {
-                mbar_arrive(&aux->mb_accfree);
-                TC_STAMP(k, 12);
+            // tile k + 3's half of the split, three tiles ahead of its GEMM 1 so that the front
+            // group never waits for it. It waits for GEMM 1 of tile k + 1 (which needs only splits
+            // made earlier; the front group issues it while this group still works on tile k) and
+            // for the tile's TMA load (issued when both groups had split tile k + 1).
+            if (k + 3 < nk && split_half(k + 3)) break;
+            if constexpr (KD <= 8) {
+                // The accumulator of tile k is freed as soon as its outputs are read: GEMM 1 of tile
+                // k + 3 waits for it, so the wait for tile k + 1's incoming state (prepare) comes
+                // after. (With 16 states this group is the slower one, and prepare(k + 1) overlapping
+                // GEMM 2 of tile k, as below, is worth more: orders 10-16 lose 3-7% this way.)
+                epilogue(k);
+                // (also: GEMM 2 of tile k has read the state operand)
+                stop = bar_group_any(2, *vbail);
+                if (stop) break;
+                if (ct == 0) {
+                    mbar_arrive(&aux->mb_accfree);
+                    TC_STAMP(k, 12);
+                }
+                if (k + 1 < nk) {
+                    prepare(k + 1);
+                    stop = bar_group_any(2, *vbail) || rescan(k + 1);  // (rows of tile k + 1 are in U)
+                }
+            } else {
+                if (k + 1 < nk) prepare(k + 1);  // overlaps GEMM 2 of tile k
+                epilogue(k);
+                // (also: rows of tile k+1 are in U, and GEMM 2 of tile k has read the state operand)
+                stop = bar_group_any(2, *vbail);
+                if (stop) break;
+                if (ct == 0) {
+                    mbar_arrive(&aux->mb_accfree);
+                    TC_STAMP(k, 12);
+                }
+                if (k + 1 < nk) stop = rescan(k + 1);
             }
-            if (k + 1 < nk) stop = rescan(k + 1);
         }
         __syncthreads();
         if (ct == 0)  // GEMM 2 batches still in flight end before TMEM is freed
