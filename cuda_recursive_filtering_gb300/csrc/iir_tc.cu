@@ -83,6 +83,7 @@ constexpr int TC_LB_MAX = 4;              // deepest truncated lookback (tiles)
 
 struct TcParams {
     CUtensorMap tmap_x;          // x as [n/64 rows][64], box {32, 128}, 128-byte swizzle
+    CUtensorMap tmap_y;          // y, the same way (output tiles leave by TMA stores)
     const float* x;
     float* y;
     long long n;
@@ -101,6 +102,7 @@ struct TcParams {
     unsigned int carry_cap;
     int D;
     int use_tma;
+    int use_tma_y;               // tmap_y is valid
     int y_vec;                   // y is 16-byte aligned
     int lb_depth;                // truncated lookback depth m (||Q^m|| <= 1e-10), 0: full lookback
     unsigned long long* prof;
@@ -459,6 +461,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     // rescan takes twice the steps and the front's split stays whole, which balances the groups
     // better (order 8: 334 -> 358 GS/s shared; order 16: 275 shared).
     auto shared_split = [&](uint32_t kk) { return BF == 0 && KD <= 8 && bulk(kk); };
+    // a whole output tile leaves by TMA stores (else the back group stores it from registers)
+    auto bulk_y = [&](uint32_t kk) {
+        return p.use_tma_y && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
+    };
 
     if (warp < TC_LBW) {
         // ================= lookback warps: tiles k = warp, warp + TC_LBW, ... =================
@@ -991,7 +997,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 tc_give_up(aux, p, epoch, IIR_DEV_ERR_MBARRIER);
             tc_fence_after();
             if (ct == 0) TC_STAMP(kk, 11);
-            if (__all_sync(0xffffffffu, ok)) {
+            if (__all_sync(0xffffffffu, ok) && bulk_y(kk)) {
+                // a whole tile: this thread's 32 outputs (chunk row 32 q + lane, k-block hh) into the
+                // state operand's buffer, free from GEMM 2 until the next rescan, in the tensor
+                // map's 128-byte swizzled layout; store_tile sends it out after the group barrier
+                float v[32];
+                __syncwarp();
+                tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>((kk % TC_NACC) * TC_ACC + 32 * hh), v);
+                float4* row = reinterpret_cast<float4*>(a2s + hh * TC_KB + (32 * q + lane) * 32);
+#pragma unroll
+                for (int g = 0; g < 8; ++g) row[g ^ (lane & 7)] = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
+                fence_proxy_async_smem();
+            } else if (__all_sync(0xffffffffu, ok)) {
                 const long long ts = static_cast<long long>(tile_of(kk)) * TC_TILE;
                 float v[32];
                 __syncwarp();
@@ -1022,6 +1039,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             tc_fence_before();
         };
 
+        // After the group barrier that follows epilogue(kk): the staged tile leaves by two TMA
+        // stores (one per k-block); the issuing thread waits until they have read the buffer,
+        // which the next rescan overwrites only after a later group barrier.
+        auto store_tile = [&](uint32_t kk) {
+            if (ct == 0 && bulk_y(kk)) {
+                const int row0 = static_cast<int>(tile_of(kk) * TC_NB);
+                tma_store_2d(&p.tmap_y, 0, row0, a2s);
+                tma_store_2d(&p.tmap_y, 32, row0, a2s + TC_KB);
+                bulk_commit();
+                bulk_wait_read_all();
+            }
+        };
         bool stop = false;
         for (uint32_t kk = 0; kk < 3 && kk < nk && !stop; ++kk) stop = split_half(kk);
         if (nk > 0 && !stop) {
@@ -1043,6 +1072,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 // (also: GEMM 2 of tile k has read the state operand)
                 stop = bar_group_any(2, *vbail);
                 if (stop) break;
+                store_tile(k);  // (the barrier before rescan(k + 1) follows prepare)
                 if (ct == 0) {
                     mbar_arrive(&aux->mb_accfree);
                     TC_STAMP(k, 12);
@@ -1061,9 +1091,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                     mbar_arrive(&aux->mb_accfree);
                     TC_STAMP(k, 12);
                 }
+                if (bulk_y(k)) {
+                    store_tile(k);
+                    bar_group(2);  // the stores have read the buffer that rescan(k + 1) rewrites
+                }
                 if (k + 1 < nk) stop = rescan(k + 1);
             }
         }
+        if (ct == 0) bulk_wait_all();  // the output tiles' TMA stores have completed
         __syncthreads();
         if (ct == 0)  // GEMM 2 batches still in flight end before TMEM is freed
             while (g2_par < aux->g2_issued && wait_mbar_bounded(&aux->mb_g2, g2_par & 1u, p.timeout_ns)) ++g2_par;
@@ -1602,6 +1637,7 @@ int tc_plan_execute(TcPlan* t, const float* x, float* y, size_t n, long long tim
     q.carry_cap = static_cast<unsigned int>(t->carry_cap);
     q.D = t->D;
     q.use_tma = encode_chunk_rows_map(&q.tmap_x, x, static_cast<long long>(n)) ? 1 : 0;
+    q.use_tma_y = encode_chunk_rows_map(&q.tmap_y, y, static_cast<long long>(n)) ? 1 : 0;
     q.y_vec = (reinterpret_cast<uintptr_t>(y) & 15u) == 0 ? 1 : 0;
     q.prof = t->prof;
     void* args[] = {&q};
