@@ -1040,16 +1040,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
         };
 
         // After the group barrier that follows epilogue(kk): the staged tile leaves by two TMA
-        // stores (one per k-block); the issuing thread waits until they have read the buffer,
-        // which the next rescan overwrites only after a later group barrier.
+        // stores (one per k-block). The issuing thread waits until they have read the buffer
+        // (store_read) before the group barrier after which the next rescan overwrites it.
         auto store_tile = [&](uint32_t kk) {
             if (ct == 0 && bulk_y(kk)) {
                 const int row0 = static_cast<int>(tile_of(kk) * TC_NB);
                 tma_store_2d(&p.tmap_y, 0, row0, a2s);
                 tma_store_2d(&p.tmap_y, 32, row0, a2s + TC_KB);
                 bulk_commit();
-                bulk_wait_read_all();
             }
+        };
+        auto store_read = [&]() {
+            if (ct == 0) bulk_wait_read_all();
         };
         bool stop = false;
         for (uint32_t kk = 0; kk < 3 && kk < nk && !stop; ++kk) stop = split_half(kk);
@@ -1072,13 +1074,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 // (also: GEMM 2 of tile k has read the state operand)
                 stop = bar_group_any(2, *vbail);
                 if (stop) break;
-                store_tile(k);  // (the barrier before rescan(k + 1) follows prepare)
                 if (ct == 0) {
                     mbar_arrive(&aux->mb_accfree);
                     TC_STAMP(k, 12);
                 }
+                store_tile(k);  // read out while prepare runs
                 if (k + 1 < nk) {
                     prepare(k + 1);
+                    store_read();
                     stop = bar_group_any(2, *vbail) || rescan(k + 1);  // (rows of tile k + 1 are in U)
                 }
             } else {
@@ -1093,6 +1096,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
                 }
                 if (bulk_y(k)) {
                     store_tile(k);
+                    store_read();
                     bar_group(2);  // the stores have read the buffer that rescan(k + 1) rewrites
                 }
                 if (k + 1 < nk) stop = rescan(k + 1);
