@@ -436,8 +436,8 @@ def run_batching(dev) -> dict:
 
 
 def run_precision(dev, log2n: int, hbm_gbs: float) -> dict:
-    """Precision form (kernel TC: the chunk solve as tcgen05 TF32 GEMMs with split products; and
-    its GEMM 1 with BF16 split operands, TC_BF16x6 and TC_BF16x3)
+    """Precision form (kernel TC: the chunk solve as tcgen05 GEMMs with split products; TC is the
+    default operand form, TC_TF32 / TC_BF16x6 / TC_BF16x3 force GEMM 1's)
     against the plain PH and STCR_UNROLL realizations on the precision workload: butter(order,
     0.05) on N(0,1) noise plus 8 tones spanning 60 dB (seed 2), orders 8..16, device-resident,
     CUDA events over 5 launches each; max|err| / RMS(ref) over ALL outputs against the FP64
@@ -461,11 +461,13 @@ def run_precision(dev, log2n: int, hbm_gbs: float) -> dict:
             sos = workloads.butter_sos(order, 0.05)
             ref = DeviceRef(gold.get(order), dev)
             row = {}
-            for kname, b, nb in (("TC", 0, 0), ("TC_BF16x6", 0, 0), ("TC_BF16x3", 0, 0), ("PH", 32, 64),
+            for kname, b, nb in (("TC", 0, 0), ("TC_TF32", 0, 0), ("TC_BF16x6", 0, 0), ("TC_BF16x3", 0, 0), ("PH", 32, 64),
                                  ("STCR_UNROLL", 32, 64)):
-                # TC_BF16x6 / x3: GEMM 1 with BF16 operands, three parts and six products / two parts
-                # and three products (IIR_GB300_TC_BF16, read when the plan is created)
-                bf = kname.split("x")[-1] if kname.startswith("TC_BF16") else None
+                # TC_TF32: GEMM 1 with TF32 hi / lo operands; TC_BF16x6 / x3: with BF16 operands,
+                # three parts and six products / two parts and three products (IIR_GB300_TC_BF16,
+                # read when the plan is created; the default takes BF16x6 for 5..8 states)
+                bf = ("0" if kname == "TC_TF32" else
+                      kname.split("x")[-1] if kname.startswith("TC_BF16") else None)
                 if bf:
                     os.environ["IIR_GB300_TC_BF16"] = bf
                 try:

@@ -490,13 +490,13 @@ int default_geometry(int kind, int n_sections, int& B, int& N) {
 }
 
 // Fastest realization by order, measured on GB300 at 2^28 samples (butter(order, 0.05), N(0,1)
-// noise plus tones): PH up to order 12 (770 / 614 / 389 / 328 / 283 GS/s at orders 2 / 4 / 8 /
-// 10 / 12; the precision form gives 314 / 276 / 276 at orders 8 / 10 / 12); the precision form
-// from order 14, its cost nearly flat in the order while PH's grows with the sections (orders
-// 14 / 16: 279 / 284 against 248 / 221 GS/s, with a quarter of the error).
+// noise plus tones): PH up to order 10 (473 / 376 GS/s at orders 8 / 10; the precision form gives
+// 438 / 307); the precision form from order 12, its cost nearly flat in the order while PH's grows
+// with the sections (orders 12 / 14 / 16: 307 / 311 / 342 against 302 / 266 / 237 GS/s, with a
+// quarter of the error).
 int resolve_auto(int kernel, int n_sections) {
     if (kernel != IIR_KERNEL_AUTO) return kernel;
-    return n_sections >= 7 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
+    return n_sections >= 6 ? IIR_KERNEL_TC : IIR_KERNEL_PH;
 }
 
 // samples per block (= per lookback unit) of the plan's large-signal kernel, or of kernel e

@@ -46,7 +46,7 @@ extern "C" {
 
 /* ---- realizations (reference: include/{ph,stcr,dtcr,plr}_kernels.cuh) ----------- */
 #define IIR_KERNEL_AUTO         0   /* fastest realization for the order, measured on GB300:
-                                       PH to order 12, the precision form (TC) from order 14 */
+                                       PH to order 10, the precision form (TC) from order 12 */
 #define IIR_KERNEL_PH           1   /* PH_32 / PH_64                      ph_kernels.cuh:208,501   */
 #define IIR_KERNEL_STCR         2   /* STCR_*_LOOP (loop-form back-sub)   stcr_kernels.cuh:279,2586 */
 #define IIR_KERNEL_STCR_UNROLL  3   /* STCR_*_UNROLL_* (register form)    stcr_kernels.cuh:608-3605 */

@@ -114,12 +114,14 @@ def test_tc_cheby1(order, cutoff, cuda_device):
 
 
 @pytest.mark.parametrize("order", (8, 16))
-@pytest.mark.parametrize("form", ("6", "3"))
+@pytest.mark.parametrize("form", ("6", "3", "0"))
 def test_tc_bf16_split_forms(order, form, monkeypatch, cuda_device):
-    """GEMM 1 with BF16 split operands (IIR_GB300_TC_BF16, read when the plan is created) on the
-    precision workload, including ragged sizes. Three parts and six products keep the float32
-    bar (max|err| / RMS <= 1e-5); two parts and three products keep the reference's gate
-    (max|err| <= 1e-4 max|ref|) at about 4e-5 RMS, so their RMS bound here is 1e-4."""
+    """GEMM 1's operand form forced by IIR_GB300_TC_BF16 (read when the plan is created) on the
+    precision workload, including ragged sizes: BF16 split operands with three parts and six
+    products (the default up to 8 states) keep the float32 bar (max|err| / RMS <= 1e-5), as
+    TF32 hi / lo operands ("0", the default with 16 states) do; two parts and three products keep
+    the reference's gate (max|err| <= 1e-4 max|ref|) at about 4e-5 RMS, so their RMS bound here
+    is 1e-4."""
     from scipy import signal
     sos = signal.butter(order, 0.05, output="sos")
     monkeypatch.setenv("IIR_GB300_TC_BF16", form)
