@@ -114,9 +114,9 @@ struct BatchBlock {
     // Bulk L2 prefetch of chunk c's whole 16-byte granules (those inside its segment).
     __device__ static void prefetch_chunk(const IirBatchParams& p, uint32_t c) {
         const IirBatchSegment& sg = p.segs[__ldg(p.chunk_seg + c)];
-        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
+        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK - sg.lead;
         const long long ce = cs + CHUNK < sg.n ? cs + CHUNK : sg.n;
-        const uintptr_t a = (reinterpret_cast<uintptr_t>(sg.x + cs) + 15u) & ~static_cast<uintptr_t>(15u);
+        const uintptr_t a = (reinterpret_cast<uintptr_t>(sg.x + (cs > 0 ? cs : 0)) + 15u) & ~static_cast<uintptr_t>(15u);
         const uintptr_t b = reinterpret_cast<uintptr_t>(sg.x + ce) & ~static_cast<uintptr_t>(15u);
         if (b > a) prefetch_l2_bulk(reinterpret_cast<const void*>(a), static_cast<uint32_t>(b - a));
     }
@@ -198,8 +198,17 @@ struct BatchBlock {
     // moves sample by sample. Completion: the caller's cp_async_wait and barrier.
     __device__ static void stage(const IirBatchParams& p, uint32_t c, uint32_t seg, float* buf, int tid) {
         const IirBatchSegment& sg = p.segs[seg];
-        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK;
+        // chunk position i holds segment sample cs + i (cs < 0: the first chunk's leading zeros)
+        const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK - sg.lead;
         const long long nrem = sg.n - cs;  // > 0
+        if (cs < 0) {
+#pragma unroll 4
+            for (int i = tid; i < CHUNK; i += THREADS) {
+                const bool in = i >= -cs && i < nrem;
+                cp_async4(buf + swz<N, ROWS, true>(i / N, i % N), in ? sg.x + (cs + i) : sg.x, in ? 4 : 0);
+            }
+            return;
+        }
         const float* src = sg.x + cs;
         const uintptr_t mis = reinterpret_cast<uintptr_t>(src) & 15u;
         if (nrem >= CHUNK && mis == 0) {
@@ -226,7 +235,7 @@ struct BatchBlock {
         const IirBatchSegment sg = p.segs[seg];
         const IirBatchFilter flt = p.filters[sg.filter];
         const uint32_t lc = c - sg.chunk0;
-        const long long cs = static_cast<long long>(lc) * CHUNK;
+        const long long cs = static_cast<long long>(lc) * CHUNK - sg.lead;  // segment sample at position 0
         const long long nrem = sg.n - cs;  // samples of the segment from this chunk's start (> 0)
 
         const bool row_warp = warp > 0;
@@ -379,7 +388,10 @@ struct BatchBlock {
         __syncthreads();
         const long long cnt = nrem < CHUNK ? nrem : CHUNK;
         const uintptr_t ymis = reinterpret_cast<uintptr_t>(sg.y + cs) & 15u;
-        if (cnt == CHUNK && ymis == 0) {
+        if (cs < 0) {  // the first chunk of a segment with leading zeros: its own samples only
+            for (long long i = tid - cs; i < cnt; i += THREADS)
+                sg.y[cs + i] = buf[swz<N, ROWS, true>(static_cast<int>(i) / N, static_cast<int>(i) % N)];
+        } else if (cnt == CHUNK && ymis == 0) {
             float4* dst = reinterpret_cast<float4*>(sg.y + cs);
             for (int i = tid; i < CHUNK / 4; i += THREADS)
                 dst[i] = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, true>((4 * i) / N, (4 * i) % N));
@@ -672,9 +684,19 @@ int batch_launch(const iir_batch* b, int k, IirBatchParams& q, cudaStream_t stre
 }
 
 // chunks of a segment of n samples with shape k
-size_t seg_chunks(size_t n, int k) {
+// Leading zeros of a segment's first chunk: a segment that starts at rest (no zi) with x not on
+// a 16-byte boundary is chunked on x's 16-byte grid, its first chunk starting 1..3 zero samples
+// before it (zero input from a zero state leaves the state zero, so the zeros change nothing). Its
+// later chunks then start 16-byte aligned and move by the 16-byte copies.
+int seg_lead(const iir_segment& s) {
+    if (s.zi || s.n == 0) return 0;
+    return static_cast<int>((reinterpret_cast<uintptr_t>(s.x) >> 2) & 3u);
+}
+
+size_t seg_chunks(const iir_segment& s, int k) {
     const ShapeDef& sd = shapes()[static_cast<size_t>(k)];
     const size_t chunk = static_cast<size_t>(sd.rows) * sd.n;
+    const size_t n = s.n == 0 ? 0 : s.n + static_cast<size_t>(seg_lead(s));
     return (n + chunk - 1) / chunk;
 }
 
@@ -779,7 +801,7 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
         const char* xb = reinterpret_cast<const char*>(s.x);
         const char* yb = reinterpret_cast<const char*>(s.y);
         if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
-        const size_t ch = seg_chunks(s.n, k);
+        const size_t ch = seg_chunks(s, k);
         total += ch;
         groups += (ch + IIR_GROUP - 1) / IIR_GROUP;
     }
@@ -812,9 +834,9 @@ int iir_batch_execute(iir_batch* b, const iir_segment* segs, int n_segs, void* s
     const size_t tail_min = batch_tail_min_chunks();
     for (int i = 0; i < n_segs; ++i) {
         const iir_segment& s = segs[i];
-        const unsigned int ch = static_cast<unsigned int>(seg_chunks(s.n, k));
+        const unsigned int ch = static_cast<unsigned int>(seg_chunks(s, k));
         hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, chunk0, group0, s.filter,
-                                ch >= tail_min ? 1 : 0};
+                                ch >= tail_min ? 1 : 0, seg_lead(s), 0};
         hstart[i] = chunk0;
         chunk0 += ch;
         group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;
@@ -858,9 +880,9 @@ int iir_batch_bind(iir_batch* b, const iir_segment* segs, int n_segs, iir_batch_
         const char* xb = reinterpret_cast<const char*>(s.x);
         const char* yb = reinterpret_cast<const char*>(s.y);
         if (s.n > 0 && xb < yb + s.n * sizeof(float) && yb < xb + s.n * sizeof(float)) return IIR_ERR_INVALID_ARGUMENT;
-        const size_t ch = seg_chunks(s.n, k);
+        const size_t ch = seg_chunks(s, k);
         hs[i] = IirBatchSegment{s.x, s.y, static_cast<long long>(s.n), s.zi, s.zf, static_cast<unsigned int>(chunk0),
-                                static_cast<unsigned int>(group0), s.filter, ch >= tail_min ? 1 : 0};
+                                static_cast<unsigned int>(group0), s.filter, ch >= tail_min ? 1 : 0, seg_lead(s), 0};
         starts[i] = static_cast<unsigned int>(chunk0);
         chunk0 += ch;
         group0 += (ch + IIR_GROUP - 1) / IIR_GROUP;

@@ -153,6 +153,9 @@ struct IirBatchSegment {
     unsigned int group0;    // first group slot of the segment
     int filter;
     int tail_ok;            // long enough for its filter's tail-aggregate schedule (host's choice)
+    int lead;               // zero samples before the segment in its first chunk (0..3): a segment
+                            // at rest whose x is not 16-byte aligned is chunked on x's 16-byte grid
+    int pad;
 };
 
 struct IirBatchParams {

@@ -361,3 +361,37 @@ def test_segments_at_every_float_offset(shape, cuda_device):
         _check(yh[b:b + n], x[a:a + n], filters[f][1], filters[f][0], (shape, i, n, a % 4, b % 4))
         covered[b:b + n] = True
     assert np.isnan(yh[~covered]).all()
+
+
+@pytest.mark.parametrize("shape", [(128, 64), (64, 16)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_segments_from_rest_at_every_offset_carry_their_state(shape, cuda_device):
+    """Segments that start at rest (no zi) at every offset modulo 16 bytes, with a final state:
+    such a segment is chunked on its input's 16-byte grid, its first chunk padded with leading
+    zeros. A second launch continues each one from its zf over the rest of its signal (that
+    launch's segments have a zi, so they keep the segment-aligned chunking), and the two pieces
+    join into the whole-signal output."""
+    filters = _mixed_filters()
+    batch = Batch([s for _, s in filters])
+    batch.set_shape(*shape)
+    chunk = batch.shape()["chunk"]
+    rng = np.random.default_rng(41 + shape[1])
+    firsts = [1, 2, 3, 5, chunk - 3, chunk - 1, chunk, chunk + 2, 3 * chunk + 1, 4 * chunk - 2]
+    firsts = [n for n in firsts for _ in range(2)]
+    rests = [int(v) for v in rng.integers(1, 3 * chunk, len(firsts))]
+    xo, p = [], 0
+    for i, (a, b) in enumerate(zip(firsts, rests)):
+        p += 1 + i % 4
+        xo.append(p)
+        p += a + b
+    x = rng.uniform(-1, 1, p + 8).astype(np.float32)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.full_like(xt, float("nan"))
+    fl = [i % len(filters) for i in range(len(firsts))]
+    st = [torch.full((batch.state_size(f),), float("nan"), device="cuda") for f in fl]
+    batch([(xt[o:o + a], yt[o:o + a], f, None, z) for o, a, f, z in zip(xo, firsts, fl, st)])
+    assert {xt[o:].data_ptr() % 16 for o in xo} == {0, 4, 8, 12}
+    batch([(xt[o + a:o + a + b], yt[o + a:o + a + b], f, z) for o, a, b, f, z in zip(xo, firsts, rests, fl, st)])
+    batch.check()
+    yh = yt.cpu().numpy()
+    for i, (o, a, b, f) in enumerate(zip(xo, firsts, rests, fl)):
+        _check(yh[o:o + a + b], x[o:o + a + b], filters[f][1], filters[f][0], (shape, i, a, b, o % 4))
