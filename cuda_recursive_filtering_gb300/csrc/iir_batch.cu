@@ -201,6 +201,28 @@ struct BatchBlock {
         // chunk position i holds segment sample cs + i (cs < 0: the first chunk's leading zeros)
         const long long cs = static_cast<long long>(c - sg.chunk0) * CHUNK - sg.lead;
         const long long nrem = sg.n - cs;  // > 0
+        const uintptr_t mis = (reinterpret_cast<uintptr_t>(sg.x) + static_cast<uintptr_t>(4 * cs)) & 15u;
+        if ((cs < 0 || nrem < CHUNK) && mis == 0) {
+            // a segment's first chunk with leading zeros, or its last chunk, on a 16-byte boundary:
+            // whole granules inside the segment as 16-byte copies, granules outside it zeroed, the
+            // granules it cuts sample by sample
+#pragma unroll 1
+            for (int g = tid; g < CHUNK / 4; g += THREADS) {
+                float* dst = buf + swz<N, ROWS, true>((4 * g) / N, (4 * g) % N);
+                const long long i0 = 4 * g;
+                if (i0 >= -cs && i0 + 3 < nrem) {
+                    cp_async16(dst, sg.x + (cs + i0));
+                } else if (i0 + 3 < -cs || i0 >= nrem) {
+                    *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+                } else {
+                    for (int t = 0; t < 4; ++t) {
+                        const bool in = i0 + t >= -cs && i0 + t < nrem;
+                        cp_async4(dst + t, in ? sg.x + (cs + i0 + t) : sg.x, in ? 4 : 0);
+                    }
+                }
+            }
+            return;
+        }
         if (cs < 0) {
 #pragma unroll 4
             for (int i = tid; i < CHUNK; i += THREADS) {
@@ -210,7 +232,6 @@ struct BatchBlock {
             return;
         }
         const float* src = sg.x + cs;
-        const uintptr_t mis = reinterpret_cast<uintptr_t>(src) & 15u;
         if (nrem >= CHUNK && mis == 0) {
 #pragma unroll 4
             for (int i = tid; i < CHUNK / 4; i += THREADS)
@@ -387,8 +408,24 @@ struct BatchBlock {
         if (live) Ph::correct_pass(buf, r, pa1, pa2, d2, d1);
         __syncthreads();
         const long long cnt = nrem < CHUNK ? nrem : CHUNK;
-        const uintptr_t ymis = reinterpret_cast<uintptr_t>(sg.y + cs) & 15u;
-        if (cs < 0) {  // the first chunk of a segment with leading zeros: its own samples only
+        const uintptr_t ymis = (reinterpret_cast<uintptr_t>(sg.y) + static_cast<uintptr_t>(4 * cs)) & 15u;
+        if ((cs < 0 || cnt < CHUNK) && ymis == 0) {
+            // a first chunk with leading zeros or a last chunk on a 16-byte boundary: whole
+            // granules of the segment's samples as 16-byte stores, the granules it cuts sample by
+            // sample
+            for (int g = tid; g < CHUNK / 4; g += THREADS) {
+                const long long i0 = 4 * g;
+                if (i0 + 3 < -cs || i0 >= cnt) continue;
+                const float4 v = *reinterpret_cast<const float4*>(buf + swz<N, ROWS, true>((4 * g) / N, (4 * g) % N));
+                if (i0 >= -cs && i0 + 3 < cnt) {
+                    *reinterpret_cast<float4*>(sg.y + (cs + i0)) = v;
+                } else {
+                    const float e[4] = {v.x, v.y, v.z, v.w};
+                    for (int t = 0; t < 4; ++t)
+                        if (i0 + t >= -cs && i0 + t < cnt) sg.y[cs + i0 + t] = e[t];
+                }
+            }
+        } else if (cs < 0) {  // the first chunk of a segment with leading zeros: its own samples only
             for (long long i = tid - cs; i < cnt; i += THREADS)
                 sg.y[cs + i] = buf[swz<N, ROWS, true>(static_cast<int>(i) / N, static_cast<int>(i) % N)];
         } else if (cnt == CHUNK && ymis == 0) {
