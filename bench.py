@@ -659,6 +659,38 @@ def run_small(dev, hbm_gbs: float) -> dict:
         rows[key] = dict(row_entry(n / (p20 * 1e-3) / 1e9, hbm_gbs, e),
                          gsps_median=round(n / (statistics.median(ms) * 1e-3) / 1e9, 1),
                          us_per_launch_p20=round(p20 * 1e3, 2))
+    # the same launches from a captured CUDA graph (200 launches over the rotating buffers per
+    # replay, 20 replays): the host's launch cost leaves the measured time
+    for kname, b, nb in (("PH", 32, 64), ("DTCR_UNROLL", 32, 64)):
+        pl = Plan(sos, kname, b, nb, max_n=n, device=dev)
+        side = torch.cuda.Stream()
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            for i in range(3):
+                pl(xs[i % nbuf], ys[i % nbuf])
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            for i in range(200):
+                pl(xs[i % nbuf], ys[i % nbuf])
+        graph.replay()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(20):
+            s0, e0 = torch.cuda.Event(True), torch.cuda.Event(True)
+            s0.record(stream)
+            graph.replay()
+            e0.record(stream)
+            torch.cuda.synchronize()
+            ms.append(s0.elapsed_time(e0) / 200)
+        pl.check()
+        e = oracle.errors(ys[0].cpu().numpy(), ref)
+        del graph
+        pl.close()
+        p20 = sorted(ms)[len(ms) // 5]
+        rows[f"order2_{kname}_{b}x{nb}_graph"] = dict(
+            row_entry(n / (p20 * 1e-3) / 1e9, hbm_gbs, e),
+            gsps_median=round(n / (statistics.median(ms) * 1e-3) / 1e9, 1), us_per_launch_p20=round(p20 * 1e3, 2))
     # the reference's own kernels on the same buffers and timing (oracle/refgpu.py)
     from oracle import refgpu
     if refgpu.available():
@@ -676,7 +708,8 @@ def run_small(dev, hbm_gbs: float) -> dict:
         del xsg
     del xs, ys
     return {"rows": rows, "method": f"{nbuf} identical input and output buffers cycled, 20 batches of 200 launches; "
-                                    "gsps = 20th-percentile batch, gsps_median = median batch"}
+                                    "gsps = 20th-percentile batch, gsps_median = median batch; *_graph rows: the "
+                                    "200 launches of a batch replayed from a captured CUDA graph"}
 
 
 def run_ours(args, rank: int, world: int, local_rank: int) -> None:
