@@ -42,6 +42,12 @@
 #include "iir_registry.h"
 #include "iir_tail.cuh"
 
+// Resident blocks per SM the batch kernel is compiled for (its register budget), at most what
+// shared memory allows.
+#ifndef IIR_BATCH_MIN_BLOCKS
+#define IIR_BATCH_MIN_BLOCKS 6
+#endif
+
 namespace iirgb {
 
 struct BatchAux {
@@ -64,7 +70,7 @@ struct BatchBlock {
     static constexpr size_t SMEM_BYTES = CHUNK * sizeof(float) + sizeof(BatchAux) + 16;
     // resident blocks per SM the kernel is compiled for (registers), at most what shared memory allows
     static constexpr int SMEM_BLOCKS = static_cast<int>((228 * 1024) / (SMEM_BYTES + 1024));
-    static constexpr int MIN_BLOCKS = SMEM_BLOCKS < 6 ? SMEM_BLOCKS : 6;
+    static constexpr int MIN_BLOCKS = SMEM_BLOCKS < IIR_BATCH_MIN_BLOCKS ? SMEM_BLOCKS : IIR_BATCH_MIN_BLOCKS;
     // tail pieces a chunk of this shape takes: one per warp, at most half of the chunk
     static constexpr int MAX_PIECES_RAW = WARPS < IIR_TAIL_MAX_PIECES ? WARPS : IIR_TAIL_MAX_PIECES;
     static constexpr int MAX_PIECES = MAX_PIECES_RAW < CHUNK / (2 * IIR_TAIL_PIECE) ? MAX_PIECES_RAW
