@@ -84,10 +84,11 @@ def test_tc_slow_decay_full_lookback(cuda_device):
     _check(y.cpu().numpy(), x, sos, rms_tol=1e-4)
 
 
-@pytest.mark.parametrize("order", (2, 16))
+@pytest.mark.parametrize("order", (2, 8, 16))
 def test_tc_long_signal(order, cuda_device):
     """2^26 + 12345 samples: about 54 tiles per block, so every hand-off slot, x buffer and
-    accumulator of the tile pipeline is reused many times within one launch."""
+    accumulator of the tile pipeline is reused many times within one launch (order 8: the
+    tile split shared by both compute groups, the BF16 form of GEMM 1)."""
     from scipy import signal
     sos = signal.butter(order, 0.05, output="sos")
     n = (1 << 26) + 12345
