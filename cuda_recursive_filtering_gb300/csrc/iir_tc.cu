@@ -36,6 +36,15 @@
 #include "iir_lookk.cuh"
 #include "iir_pipe.cuh"
 
+// Largest carried-state count whose tiles the two compute groups split in halves and whose back
+// group frees an accumulator before preparing the next tile. The two go together: the shared
+// split is validated only with that order (with the other order, preparation first, it gave wrong
+// output at 16 states in a trial). Measured at 2^28: faster up to 8 states (order 8: 358 against
+// 334 GS/s), slower at 16 (orders 10 / 16: 302 / 336 against 307 / 342 GS/s).
+#ifndef IIR_TC_SHARED_MAX_KD
+#define IIR_TC_SHARED_MAX_KD 8
+#endif
+
 namespace iirgb {
 
 constexpr int TC_L = 64;                  // samples per chunk (GEMM K)
@@ -460,7 +469,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
     // whole by the front group, which then arrives for both. With 16 states the back group's
     // rescan takes twice the steps and the front's split stays whole, which balances the groups
     // better (order 8: 334 -> 358 GS/s shared; order 16: 275 shared).
-    auto shared_split = [&](uint32_t kk) { return BF == 0 && KD <= 8 && bulk(kk); };
+    auto shared_split = [&](uint32_t kk) { return BF == 0 && KD <= IIR_TC_SHARED_MAX_KD && bulk(kk); };
     // a whole output tile leaves by TMA stores (else the back group stores it from registers)
     auto bulk_y = [&](uint32_t kk) {
         return p.use_tma_y && static_cast<long long>(tile_of(kk) + 1) * TC_TILE <= p.n;
@@ -1065,7 +1074,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) iir_tc_kernel(const __grid_cons
             // made earlier; the front group issues it while this group still works on tile k) and
             // for the tile's TMA load (issued when both groups had split tile k + 1).
             if (k + 3 < nk && split_half(k + 3)) break;
-            if constexpr (KD <= 8) {
+            if constexpr (KD <= IIR_TC_SHARED_MAX_KD) {
                 // The accumulator of tile k is freed as soon as its outputs are read: GEMM 1 of tile
                 // k + 3 waits for it, so the wait for tile k + 1's incoming state (prepare) comes
                 // after. (With 16 states this group is the slower one, and prepare(k + 1) overlapping
