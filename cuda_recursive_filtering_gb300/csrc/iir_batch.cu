@@ -199,9 +199,10 @@ struct BatchBlock {
     }
 
     // All threads: start copying chunk c of segment `seg` into buf (cp.async, no registers held),
-    // zero past the segment's end. Whole chunks move as 16-byte copies when the chunk starts on a
-    // 16-byte boundary, else as 8- or 4-byte copies per 16-byte granule; the segment's last chunk
-    // moves sample by sample. Completion: the caller's cp_async_wait and barrier.
+    // zero before the segment's start (a first chunk's leading zeros) and past its end. A chunk on
+    // the 16-byte grid moves its whole granules as 16-byte copies; a whole chunk off the grid (a
+    // segment with an initial state, not 16-byte aligned) as 8- or 4-byte copies per granule; the
+    // rest sample by sample. Completion: the caller's cp_async_wait and barrier.
     __device__ static void stage(const IirBatchParams& p, uint32_t c, uint32_t seg, float* buf, int tid) {
         const IirBatchSegment& sg = p.segs[seg];
         // chunk position i holds segment sample cs + i (cs < 0: the first chunk's leading zeros)
